@@ -1,0 +1,363 @@
+// Single-modulus engine behind the kc_* C ABI (include/kite_cuda.h).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "../../include/kite_cuda.h"
+#include "kernels.h"
+#include "layout.h"
+#include "plan.h"
+
+using namespace kg;
+
+struct kc_engine {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    Layout lay;
+    std::shared_ptr<LengthPlan> plan;
+    TestDesc desc{};
+    TestDesc *d_desc = nullptr;
+    WorkItem *d_work = nullptr;  // rows then columns
+    LaunchSet ls;
+    uint8_t *d_bits = nullptr;
+    double *d_w = nullptr, *d_osc = nullptr, *d_idig = nullptr;
+    long long *d_dig = nullptr, *d_slot = nullptr;
+    unsigned long long *d_maxerr = nullptr;
+    int *d_status = nullptr;
+    long long *h_dig = nullptr;      // pinned staging for digit transfers
+    unsigned long long *h_err = nullptr;
+    int err = 0;
+    uint32_t err_every = 1;
+    uint64_t op_count = 0;
+    int add_cached = 0;              // constant currently folded in desc (0: none)
+    int64_t add_c = 0;
+};
+
+namespace {
+
+bool ok(kc_engine *e, cudaError_t rc) {
+    if (rc != cudaSuccess && !e->err) e->err = -(int)rc;
+    return rc == cudaSuccess;
+}
+
+bool check_launch(kc_engine *e) { return ok(e, cudaGetLastError()); }
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+template <class T>
+bool dalloc(kc_engine *e, T **p, size_t count) {
+    return ok(e, cudaMalloc((void **)p, (count ? count : 1) * sizeof(T)));
+}
+
+void release(kc_engine *e) {
+    cudaFree(e->d_desc);
+    cudaFree(e->d_work);
+    cudaFree(e->d_bits);
+    cudaFree(e->d_w);
+    cudaFree(e->d_osc);
+    cudaFree(e->d_idig);
+    cudaFree(e->d_dig);
+    cudaFree(e->d_slot);
+    cudaFree(e->d_maxerr);
+    cudaFree(e->d_status);
+    if (e->h_dig) cudaFreeHost(e->h_dig);
+    if (e->h_err) cudaFreeHost(e->h_err);
+    if (e->stream) cudaStreamDestroy(e->stream);
+}
+
+bool upload_desc(kc_engine *e) {
+    return ok(e, cudaMemcpyAsync(e->d_desc, &e->desc, sizeof(TestDesc), cudaMemcpyHostToDevice, e->stream));
+}
+
+bool want_err(kc_engine *e) {
+    bool t = e->err_every <= 1 || e->op_count % e->err_every == 0;
+    e->op_count++;
+    return t;
+}
+
+// one product pass: row pass (square or multiply), then the two column kernels
+int product(kc_engine *e, double2 *x, const double2 *y) {
+    const bool track = want_err(e);
+    launch_rows(e->ls, y != nullptr, x, y);
+    launch_col_inverse(e->ls, track, x);
+    launch_col_forward(e->ls, x, true);
+    return check_launch(e) ? 0 : e->err;
+}
+
+int set_addend(kc_engine *e, int64_t c) {
+    if (e->add_cached == (c != 0) && e->add_c == c) return 0;
+    uint32_t idx[kMaxAddend];
+    int64_t val[kMaxAddend];
+    int cnt = 0;
+    if (c) {
+        cnt = e->lay.constant_digits(c, idx, val, kMaxAddend);
+        if (cnt < 0) return -1;
+    }
+    e->desc.nadd = cnt;
+    for (int i = 0; i < cnt; i++) {
+        e->desc.addj[i] = (int)idx[i];
+        e->desc.addv[i] = val[i];
+    }
+    e->add_cached = c != 0;
+    e->add_c = c;
+    return upload_desc(e) ? 0 : e->err;
+}
+
+}  // namespace
+
+extern "C" {
+
+kc_engine *kc_engine_new(uint64_t k, uint64_t n, uint32_t L, const uint8_t *bits, const double *w,
+                         const double *oscale, uint32_t top_t, uint64_t top_st, uint32_t top_m,
+                         uint64_t sL, int device) {
+    kc_engine *e = new (std::nothrow) kc_engine();
+    if (!e) return nullptr;
+    if (device < 0 && cudaGetDevice(&device) != cudaSuccess) {
+        delete e;
+        return nullptr;
+    }
+    e->device = device;
+    DeviceGuard dg(device);
+    if (!e->lay.build(k, n, L)) {
+        delete e;
+        return nullptr;
+    }
+    // a caller-provided layout must be the one this (k, n, L) defines
+    if ((bits && std::memcmp(bits, e->lay.bits.data(), L)) || (top_t && top_t != e->lay.top_t) ||
+        (top_st && top_st != e->lay.top_st) || (top_m && top_m != e->lay.top_m) || (sL && sL != e->lay.sL)) {
+        delete e;
+        return nullptr;
+    }
+    const double *wv = w ? w : e->lay.w.data();
+    const double *ov = oscale ? oscale : e->lay.oscale.data();
+    e->plan = get_plan(L);
+    if (!e->plan || e->lay.L - e->lay.top_t > 2 * (uint32_t)kGroup) {
+        delete e;
+        return nullptr;
+    }
+    const LengthPlan &P = *e->plan;
+    const uint32_t H = P.H;
+    bool good = ok(e, cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking)) &&
+                dalloc(e, &e->d_desc, 1) && dalloc(e, &e->d_work, P.pairs.size() + P.NG) &&
+                dalloc(e, &e->d_bits, L) && dalloc(e, &e->d_w, L) && dalloc(e, &e->d_osc, L) &&
+                dalloc(e, &e->d_idig, L) && dalloc(e, &e->d_dig, L) && dalloc(e, &e->d_slot, (size_t)P.NG * P.R) &&
+                dalloc(e, &e->d_maxerr, 1) && dalloc(e, &e->d_status, 1) &&
+                ok(e, cudaMallocHost((void **)&e->h_dig, (size_t)L * sizeof(long long))) &&
+                ok(e, cudaMallocHost((void **)&e->h_err, sizeof(unsigned long long)));
+    if (good) {
+        std::vector<double> osc(L), idig(L);
+        const double s4 = 1.0 / (4.0 * H);
+        for (uint32_t j = 0; j < L; j++) {
+            osc[j] = ov[j] * s4;
+            idig[j] = 1.0 / ((double)P.R * wv[j]);
+        }
+        std::vector<WorkItem> work;
+        for (size_t i = 0; i < P.pairs.size(); i++) work.push_back({0, (int)i});
+        for (uint32_t g = 0; g < P.NG; g++) work.push_back({0, (int)g});
+        good = ok(e, cudaMemcpy(e->d_bits, e->lay.bits.data(), L, cudaMemcpyHostToDevice)) &&
+               ok(e, cudaMemcpy(e->d_w, wv, L * sizeof(double), cudaMemcpyHostToDevice)) &&
+               ok(e, cudaMemcpy(e->d_osc, osc.data(), L * sizeof(double), cudaMemcpyHostToDevice)) &&
+               ok(e, cudaMemcpy(e->d_idig, idig.data(), L * sizeof(double), cudaMemcpyHostToDevice)) &&
+               ok(e, cudaMemcpy(e->d_work, work.data(), work.size() * sizeof(WorkItem), cudaMemcpyHostToDevice)) &&
+               ok(e, cudaMemset(e->d_maxerr, 0, sizeof(unsigned long long))) &&
+               ok(e, cudaMemset(e->d_status, 0, sizeof(int))) &&
+               ok(e, cudaMemset(e->d_slot, 0, (size_t)P.NG * P.R * sizeof(long long)));
+    }
+    if (good) {
+        TestDesc &d = e->desc;
+        d.L = (int)L;
+        d.H = (int)H;
+        d.R = (int)P.R;
+        d.C = (int)P.C;
+        d.NG = (int)P.NG;
+        d.rp = P.rp;
+        d.cp = P.cp;
+        d.twr = P.twr;
+        d.twc = P.twc;
+        d.t4 = P.t4;
+        d.sw = P.sw;
+        d.part0 = P.part0;
+        d.part1 = P.part1;
+        d.pairs = P.dpairs;
+        d.npairs = (int)P.pairs.size();
+        d.prow0 = 0;
+        d.bits = e->d_bits;
+        d.w = e->d_w;
+        d.osc = e->d_osc;
+        d.idig = e->d_idig;
+        d.dig = e->d_dig;
+        d.slot = e->d_slot;
+        d.maxerr = e->d_maxerr;
+        d.status = e->d_status;
+        d.k = k;
+        d.top_t = (int)e->lay.top_t;
+        d.top_m = (int)e->lay.top_m;
+        d.top_shift = (int)(e->lay.sL - e->lay.top_st);
+        d.nadd = 0;
+        d.x = nullptr;
+        d.y = nullptr;
+        good = upload_desc(e) && ok(e, cudaStreamSynchronize(e->stream));
+        LaunchSet &s = e->ls;
+        s.stream = e->stream;
+        s.tests = e->d_desc;
+        s.rows = e->d_work;
+        s.nrows = (int)P.pairs.size();
+        s.cols = e->d_work + P.pairs.size();
+        s.ncols = (int)P.NG;
+        s.grid_rows = s.nrows;
+        s.grid_cols = s.ncols;
+        s.row_smem_per_lane = (size_t)P.C * sizeof(double2);
+        s.col_smem = (size_t)P.R * kGroup * sizeof(double2);
+        good = good && kernels_prepare(s.row_smem_per_lane * 4, s.col_smem) == 0;
+    }
+    if (!good) {
+        release(e);
+        delete e;
+        return nullptr;
+    }
+    return e;
+}
+
+void kc_engine_free(kc_engine *e) {
+    if (!e) return;
+    DeviceGuard dg(e->device);
+    cudaStreamSynchronize(e->stream);
+    release(e);
+    delete e;
+}
+
+size_t kc_num_doubles(const kc_engine *e) { return e->lay.L; }
+
+double *kc_num_alloc(kc_engine *e) {
+    DeviceGuard dg(e->device);
+    double *p = nullptr;
+    if (!ok(e, cudaMalloc((void **)&p, (size_t)e->lay.L * sizeof(double)))) return nullptr;
+    if (!ok(e, cudaMemsetAsync(p, 0, (size_t)e->lay.L * sizeof(double), e->stream))) {
+        cudaFree(p);
+        return nullptr;
+    }
+    return p;
+}
+
+void kc_num_free(kc_engine *e, double *x) {
+    if (!x) return;
+    DeviceGuard dg(e->device);
+    cudaStreamSynchronize(e->stream);
+    cudaFree(x);
+}
+
+int kc_from_digits(kc_engine *e, double *x, const int64_t *digits) {
+    DeviceGuard dg(e->device);
+    const size_t L = e->lay.L;
+    if (!ok(e, cudaStreamSynchronize(e->stream))) return e->err;  // staging buffer reuse
+    std::memcpy(e->h_dig, digits, L * sizeof(long long));
+    if (!ok(e, cudaMemcpyAsync(e->d_dig, e->h_dig, L * sizeof(long long), cudaMemcpyHostToDevice, e->stream)))
+        return e->err;
+    launch_col_forward(e->ls, (double2 *)x, false);
+    return check_launch(e) ? 0 : e->err;
+}
+
+int kc_to_digits(kc_engine *e, const double *x, int64_t *digits) {
+    DeviceGuard dg(e->device);
+    const size_t L = e->lay.L;
+    launch_col_digits(e->ls, (const double2 *)x);
+    if (!check_launch(e)) return e->err;
+    if (!ok(e, cudaMemcpyAsync(e->h_dig, e->d_dig, L * sizeof(long long), cudaMemcpyDeviceToHost, e->stream)) ||
+        !ok(e, cudaStreamSynchronize(e->stream)))
+        return e->err;
+    std::memcpy(digits, e->h_dig, L * sizeof(long long));
+    return 0;
+}
+
+int kc_square(kc_engine *e, double *x, uint64_t count) {
+    DeviceGuard dg(e->device);
+    if (e->add_c && set_addend(e, 0)) return e->err ? e->err : -1;
+    for (uint64_t i = 0; i < count; i++)
+        if (product(e, (double2 *)x, nullptr)) return e->err;
+    return 0;
+}
+
+int kc_square_add(kc_engine *e, double *x, uint64_t count, int64_t c) {
+    DeviceGuard dg(e->device);
+    if (set_addend(e, c)) return e->err ? e->err : -1;
+    for (uint64_t i = 0; i < count; i++)
+        if (product(e, (double2 *)x, nullptr)) return e->err;
+    return 0;
+}
+
+int kc_mul(kc_engine *e, double *x, const double *y) {
+    DeviceGuard dg(e->device);
+    if (e->add_c && set_addend(e, 0)) return e->err ? e->err : -1;
+    return product(e, (double2 *)x, (const double2 *)y);
+}
+
+int kc_copy(kc_engine *e, double *dst, const double *src) {
+    DeviceGuard dg(e->device);
+    if (dst == src) return 0;
+    return ok(e, cudaMemcpyAsync(dst, src, (size_t)e->lay.L * sizeof(double), cudaMemcpyDeviceToDevice, e->stream))
+               ? 0
+               : e->err;
+}
+
+int kc_add(kc_engine *e, double *x, const double *y) {
+    DeviceGuard dg(e->device);
+    launch_elementwise(e->stream, (double2 *)x, (const double2 *)y, e->lay.L / 2, 1);
+    return check_launch(e) ? 0 : e->err;
+}
+
+int kc_sub(kc_engine *e, double *x, const double *y) {
+    DeviceGuard dg(e->device);
+    launch_elementwise(e->stream, (double2 *)x, (const double2 *)y, e->lay.L / 2, 2);
+    return check_launch(e) ? 0 : e->err;
+}
+
+double kc_maxerr(kc_engine *e) {
+    DeviceGuard dg(e->device);
+    if (e->err) return 1.0;
+    if (!ok(e, cudaMemcpyAsync(e->h_err, e->d_maxerr, sizeof(unsigned long long), cudaMemcpyDeviceToHost, e->stream)) ||
+        !ok(e, cudaStreamSynchronize(e->stream)))
+        return 1.0;
+    double v;
+    std::memcpy(&v, e->h_err, sizeof v);
+    return v;
+}
+
+void kc_reset_maxerr(kc_engine *e) {
+    DeviceGuard dg(e->device);
+    ok(e, cudaMemsetAsync(e->d_maxerr, 0, sizeof(unsigned long long), e->stream));
+}
+
+void kc_set_roundoff_check(kc_engine *e, uint32_t every) { e->err_every = every ? every : 1; }
+
+int kc_error(const kc_engine *e) { return e->err; }
+
+int kc_sync(kc_engine *e) {
+    DeviceGuard dg(e->device);
+    ok(e, cudaStreamSynchronize(e->stream));
+    return e->err;
+}
+
+void *kc_stream(kc_engine *e) { return (void *)e->stream; }
+
+void kc_shape(const kc_engine *e, uint32_t *R, uint32_t *C) {
+    if (R) *R = e->plan->R;
+    if (C) *C = e->plan->C;
+}
+
+}  // extern "C"

@@ -1,0 +1,37 @@
+// Host-side launch interface of the squaring kernels (kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "device.h"
+
+namespace kg {
+
+constexpr int kThreads = 256;
+
+// Everything one launch of the pass kernels needs: the test table, the work lists and the
+// grid sizes.  The same set serves a single test and a batch.
+struct LaunchSet {
+    cudaStream_t stream = nullptr;
+    const TestDesc *tests = nullptr;   // device
+    const WorkItem *rows = nullptr;    // device: row-pair work items
+    int nrows = 0;
+    const WorkItem *cols = nullptr;    // device: column-group work items
+    int ncols = 0;
+    int grid_rows = 0, grid_cols = 0;
+    size_t row_smem_per_lane = 0;      // C * sizeof(double2) for the longest row
+    size_t col_smem = 0;               // R * kGroup * sizeof(double2) for the longest column
+};
+
+// Raise the kernels' dynamic shared-memory limits; 0 on success.
+int kernels_prepare(size_t row_smem, size_t col_smem);
+
+// x, y non-null override the per-test operands (single-test use).
+void launch_rows(const LaunchSet &s, bool mul, double2 *x, const double2 *y);
+void launch_col_inverse(const LaunchSet &s, bool track_err, const double2 *x);
+void launch_col_forward(const LaunchSet &s, double2 *x, bool use_slots);
+void launch_col_digits(const LaunchSet &s, const double2 *x);
+// op: 0 copy, 1 add, 2 sub
+void launch_elementwise(cudaStream_t st, double2 *x, const double2 *y, size_t n, int op);
+
+}  // namespace kg

@@ -1,0 +1,45 @@
+// Per-FFT-length plans: four-step shape, mixed-radix stage plans and the twiddle tables, built
+// once per (device, L) on the host and kept resident on the device.
+#pragma once
+
+#include <cstdint>
+#include <memory>
+#include <vector>
+
+#include "device.h"
+
+namespace kg {
+
+struct LengthPlan {
+    uint32_t L = 0, H = 0, R = 0, C = 0, NG = 0;
+    FftPlan rp, cp;                   // row plan (C points), column plan (R points)
+    std::vector<int> rev_r, pos_r;    // DIF output position <-> frequency, column transform
+    std::vector<int> rev_c, pos_c;    // same for the row transform
+    std::vector<int2> pairs;          // row pairs (p, p'), p <= p'
+    // device copies
+    int device = -1;
+    double2 *twr = nullptr, *twc = nullptr, *t4 = nullptr, *sw = nullptr;
+    int *part0 = nullptr, *part1 = nullptr;
+    int2 *dpairs = nullptr;
+    size_t device_bytes = 0;
+    ~LengthPlan();
+};
+
+// H = R*C with C a multiple of kGroup; false if no usable shape exists.
+bool choose_shape(uint32_t H, uint32_t &R, uint32_t &C);
+// Radices for a length-n transform in DIF order; false if n has a prime factor above 7.
+bool make_fft_plan(int n, FftPlan &pl);
+
+// exp(-2 pi i j / m) with the angle reduced exactly in integer arithmetic
+double2 cis_neg(uint64_t j, uint64_t m);
+
+// Cached plan for (current device, L); nullptr if L cannot be planned or the device upload
+// fails.  Thread-safe.
+std::shared_ptr<LengthPlan> get_plan(uint32_t L);
+// Host tables only (no device upload): used by host-side tests of the plan logic.
+std::shared_ptr<LengthPlan> build_plan_host(uint32_t L, std::vector<double2> *twr,
+                                            std::vector<double2> *twc, std::vector<double2> *t4,
+                                            std::vector<double2> *sw, std::vector<int> *part0,
+                                            std::vector<int> *part1);
+
+}  // namespace kg

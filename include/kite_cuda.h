@@ -1,0 +1,93 @@
+/* C ABI of the GB300 squaring engine: the boundary a kite backend binds.
+ *
+ * The reference selects an arithmetic backend through a vtable (src/internal.h:57-66,
+ * struct kite_backend_ops {init, free, to_digits, from_digits, square, mul, mul_small}),
+ * dispatched in kite_ctx_new (src/ctx.c:256-280).  Each entry point below replaces one hook
+ * of that vtable, or one of the host loops in src/ctx.c that assume numbers live in host
+ * memory (kite_copy/add/sub, src/ctx.c:323-343; kite_max_roundoff, src/ctx.c:300).  Arguments
+ * are plain pointers and sizes; numbers are device pointers returned by kc_num_alloc.
+ *
+ * Errors: entry points returning int give 0 on success and a negative value after a CUDA
+ * failure.  A failure is sticky on the engine: kc_error() reports it and kc_maxerr() returns
+ * 1.0 from then on, which sends the reference's drivers down their retry path.  No entry point
+ * aborts the process.
+ */
+#ifndef KITE_CUDA_H
+#define KITE_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct kc_engine kc_engine;
+
+/* Replaces kite_backend_ops.init (src/internal.h:60; e.g. src/ref_fft.c:50-65).  The layout is
+ * the context's own (src/internal.h:31-54: bits, w, oscale, top_t, top_st, top_m, sL); the
+ * engine copies it to the device.  device < 0: the current CUDA device.  NULL on failure. */
+kc_engine *kc_engine_new(uint64_t k, uint64_t n, uint32_t L, const uint8_t *bits, const double *w,
+                         const double *oscale, uint32_t top_t, uint64_t top_st, uint32_t top_m,
+                         uint64_t sL, int device);
+/* Replaces kite_backend_ops.free (src/internal.h:61). */
+void kc_engine_free(kc_engine *e);
+/* Doubles per number (the reference's ctx->num_doubles, src/internal.h:53). */
+size_t kc_num_doubles(const kc_engine *e);
+
+/* Number storage in device memory: replaces kite_alloc/kite_free_aligned as used by
+ * kite_num_new/kite_num_free (src/ctx.c:305-321).  The new number is zero. */
+double *kc_num_alloc(kc_engine *e);
+void kc_num_free(kc_engine *e, double *x);
+
+/* Replace kite_backend_ops.from_digits / to_digits (src/internal.h:62-63): L balanced integer
+ * digits in host memory <-> the device number.  to_digits waits for the engine's queue. */
+int kc_from_digits(kc_engine *e, double *x, const int64_t *digits);
+int kc_to_digits(kc_engine *e, const double *x, int64_t *digits);
+
+/* Replace kite_backend_ops.square / mul (src/internal.h:64-65) and the loop of kite_square_n
+ * (src/ctx.c:329-331).  Queued on the engine's stream; return without waiting. */
+int kc_square(kc_engine *e, double *x, uint64_t count);
+int kc_mul(kc_engine *e, double *x, const double *y);
+/* x <- x^2 + c (c a small signed constant in value terms, e.g. -2 for the LLR step
+ * V <- V^2 - 2, src/llr.c:395-406), the constant folded into the carry: no extra pass. */
+int kc_square_add(kc_engine *e, double *x, uint64_t count, int64_t c);
+
+/* Replace the host loops of kite_copy / kite_add / kite_sub (src/ctx.c:323-343). */
+int kc_copy(kc_engine *e, double *dst, const double *src);
+int kc_add(kc_engine *e, double *x, const double *y);
+int kc_sub(kc_engine *e, double *x, const double *y);
+
+/* Round-off: replaces the reads and writes of ctx->maxerr (src/ctx.c:300-302) and the sampling
+ * of src/neon.c:779.  kc_maxerr waits for the queue. */
+double kc_maxerr(kc_engine *e);
+void kc_reset_maxerr(kc_engine *e);
+void kc_set_roundoff_check(kc_engine *e, uint32_t every);
+
+/* Sticky CUDA error (0 if none); kc_sync waits for the queue and returns kc_error(). */
+int kc_error(const kc_engine *e);
+int kc_sync(kc_engine *e);
+/* The engine's CUDA stream (a cudaStream_t), for callers that time or order work on it. */
+void *kc_stream(kc_engine *e);
+/* Four-step shape chosen for the engine's length: H = R * C complex points. */
+void kc_shape(const kc_engine *e, uint32_t *R, uint32_t *C);
+
+/* ---- host-only helpers (no GPU needed) ---------------------------------------------------
+ * The exact integer layer the engine's callers use, exported so a host can check or reuse it:
+ * kc_layout fills the digit layout of (k, n, L) as the reference's build_layout does
+ * (src/ctx.c:198-221): bits[L], w[L], oscale[L] and meta = {lam, sL, top_t, top_st, top_m};
+ * kc_digits_to_limbs / kc_limbs_to_digits convert as kite_get_limbs / kite_set_limbs
+ * (src/ctx.c:497-544); kc_carry_digits is kite_carry_digits (src/ctx.c:378-407).  Each returns
+ * 0, or -1 when (k, n, L) cannot be laid out. */
+int kc_layout(uint64_t k, uint64_t n, uint32_t L, uint8_t *bits, double *w, double *oscale,
+              uint64_t *meta);
+int kc_digits_to_limbs(uint64_t k, uint64_t n, uint32_t L, const int64_t *digits, uint64_t *limbs);
+int kc_limbs_to_digits(uint64_t k, uint64_t n, uint32_t L, const uint64_t *limbs, int64_t *digits);
+int kc_carry_digits(uint64_t k, uint64_t n, uint32_t L, int64_t *digits);
+/* FFT length the engine picks for (k, n) (src/ctx.c:107-141), 0 if none. */
+uint32_t kc_choose_fft_len(uint64_t k, uint64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
