@@ -1,0 +1,116 @@
+"""The C-ABI library on the CPU: it loads, exports every function include/*.h declares, and its
+exact host layer (layout, weights, carry with fold, limbs) agrees with the oracle and with exact
+integer arithmetic.  No GPU and no compute call on a device."""
+import ctypes as C
+import os
+import random
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_functions():
+    names = []
+    for h in ("kite.h", "kite_cuda.h"):
+        with open(os.path.join(ROOT, "include", h)) as f:
+            src = f.read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        src = re.sub(r"//[^\n]*", "", src)
+        for m in re.finditer(r"\b([a-z_][a-z0-9_]*)\s*\(", src):
+            name = m.group(1)
+            if name.startswith(("kite_", "kc_")) and not name.endswith("_fn"):
+                names.append(name)
+    # drop function-pointer field names inside structs
+    return sorted(set(n for n in names if n not in ("progress", "on_point", "on_confirm")))
+
+
+def test_library_exports_every_declared_function(lib):
+    declared = _declared_functions()
+    assert len(declared) > 40
+    missing = [n for n in declared if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_binding_declares_every_header_function(lib):
+    from ahnum_gb300 import native
+    assert set(_declared_functions()) <= set(native.PROTOTYPES)
+
+
+@pytest.mark.parametrize("k,n,L", [(9357, 369717, 28672), (9001, 662695, 49152), (1, 44497, 2560),
+                                   (255, 20000000, 1179648), (3, 1000, 64), (9999, 60000, 3584)])
+def test_layout_identical_to_oracle(lib, oracle_mod, k, n, L):
+    import numpy as np
+    bits = (C.c_uint8 * L)()
+    w = (C.c_double * L)()
+    osc = (C.c_double * L)()
+    meta = (C.c_uint64 * 5)()
+    assert lib.kc_layout(k, n, L, bits, w, osc, meta) == 0
+    with oracle_mod.OracleCtx(k, n, L) as o:
+        ob, ow, oo, om = o.layout()
+    assert bytes(bits) == ob
+    assert np.array_equal(np.frombuffer(w, dtype=np.float64).view(np.uint64),
+                          np.array(ow, dtype=np.float64).view(np.uint64))
+    assert np.array_equal(np.frombuffer(osc, dtype=np.float64).view(np.uint64),
+                          np.array(oo, dtype=np.float64).view(np.uint64))
+    assert list(meta) == om
+
+
+def _positions(k, n, L):
+    bits = (C.c_uint8 * L)()
+    from ahnum_gb300 import native
+    native.load().kc_layout(k, n, L, bits, None, None, None)
+    s = [0]
+    for b in bits:
+        s.append(s[-1] + b)
+    return s
+
+
+@pytest.mark.parametrize("k,n,L", [(9357, 20000, 1344), (1, 44497, 2560), (7, 5000, 512), (3, 1000, 64)])
+def test_digits_limbs_round_trip_and_carry(lib, k, n, L):
+    N = k * (1 << n) - 1
+    nl = (n + 127) // 64
+    s = _positions(k, n, L)
+    rng = random.Random(L)
+    for _ in range(5):
+        v = rng.randrange(N)
+        limbs = (C.c_uint64 * nl)(*[(v >> (64 * i)) & (2**64 - 1) for i in range(nl)])
+        d = (C.c_int64 * L)()
+        assert lib.kc_limbs_to_digits(k, n, L, limbs, d) == 0
+        # stored form is v/k: k * sum(d_j 2^{s_j}) == v (mod N)
+        assert (k * sum(int(d[j]) << s[j] for j in range(L)) - v) % N == 0
+        out = (C.c_uint64 * nl)()
+        assert lib.kc_digits_to_limbs(k, n, L, d, out) == 0
+        assert sum(int(out[i]) << (64 * i) for i in range(nl)) == v
+        # unbalanced digits (products before the carry) carry to the same value
+        big = [rng.randrange(-2**50, 2**50) for _ in range(L)]
+        d2 = (C.c_int64 * L)(*big)
+        assert lib.kc_carry_digits(k, n, L, d2) == 0
+        val = lambda dd: (k * sum(int(dd[j]) << s[j] for j in range(L))) % N
+        assert val(d2) == val(big)
+        for j in range(L - 1):
+            if j < L - 4:
+                b = s[j + 1] - s[j]
+                assert -(1 << (b - 1)) <= d2[j] < (1 << (b - 1))
+
+
+def test_choose_fft_len_matches_oracle(lib, oracle_mod):
+    rng = random.Random(7)
+    for _ in range(40):
+        k = rng.randrange(1, 10000) | 1
+        n = rng.randrange(300000, 700001)
+        assert lib.kc_choose_fft_len(k, n) == oracle_mod.choose_fft_len(k, n)
+    assert oracle_mod.choose_fft_len(9357, 369717) > 0
+
+
+def test_ctx_new_rejects_cpu_backends(lib):
+    """no CPU fallback: the reference's CPU backend ids are refused (returns NULL) without a GPU
+    being touched"""
+    from ahnum_gb300 import native
+    for b in (1, 2, 3, 4):
+        o = native.KiteOpts(b, 0, 0, 0)
+        assert not lib.kite_ctx_new(9357, 20000, -1, C.byref(o))
+    o = native.KiteOpts(5, 0, 0, 0)
+    assert not lib.kite_ctx_new(9358, 20000, -1, C.byref(o))  # even k
+    assert not lib.kite_ctx_new(9357, 20000, 1, C.byref(o))   # c != -1

@@ -1,0 +1,172 @@
+"""The CPU oracle pinned against the reference's golden vectors, GMP fixtures and exact
+integer arithmetic (no GPU).  The oracle is the checker of every GPU parity test, so it is
+checked first.
+
+Golden residues: the reference's tests/known_residues.csv (GMP rows) and the LLR results of its
+CMakeLists.txt:86-90; restated here as data.  Where the reference's own portable backends were
+built from its sources (oracle/_ref, this container only), the oracle's layout and arithmetic
+are compared with them directly.
+"""
+import ctypes as C
+import hashlib
+import json
+import os
+import random
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+KNOWN_FAST = [
+    (9357, 20000, 0x79291CD2F47CE48C),
+    (8191, 25000, 0xD45538E6F07266C6),
+    (3, 26459, 0x1),
+]
+
+
+@pytest.mark.parametrize("k,n,res", KNOWN_FAST)
+def test_oracle_known_residues(oracle_mod, k, n, res):
+    rc, r, is_prp, err = oracle_mod.fermat(k, n)
+    assert rc == 0 and r == res and is_prp == (res == 1) and err < 0.4
+
+
+@pytest.mark.parametrize("k,n,prime,res", [(3, 26459, True, 0), (9357, 20000, False, 0xDC52061161A0DE1C)])
+def test_oracle_llr(oracle_mod, k, n, prime, res):
+    rc, P, f, r, is_prime, err = oracle_mod.llr(k, n)
+    assert rc == 0 and f == 0 and is_prime == prime
+    if not prime:
+        assert r == res
+
+
+@pytest.mark.parametrize("k,n,L", [(9357, 3000, 256), (1, 5000, 512), (5, 4000, 448), (9999, 6000, 512),
+                                   (33, 2500, 320)])
+def test_oracle_gmp_protocol(oracle_mod, k, n, L):
+    """the randomized protocol of reference tests/test_gmp.c:56-172, against Python integers"""
+    rng = random.Random(k + n)
+    with oracle_mod.OracleCtx(k, n, L) as o:
+        N = o.N
+        a, b = rng.randrange(N), rng.randrange(N)
+        x, y = o.num(a), o.num(b)
+        assert o.get(x) == a
+        o.square(x, 20)
+        t = pow(a, 1 << 20, N)
+        assert o.get(x) == t
+        o.mul(x, y)
+        t = t * b % N
+        assert o.get(x) == t
+        o.mul_small(x, 3)
+        t = t * 3 % N
+        assert o.get(x) == t
+        o.add(x, y)
+        o.square(x)
+        t = (t + b) ** 2 % N
+        assert o.get(x) == t
+        o.sub(x, y)
+        t = (t - b) % N
+        assert o.get(x) == t
+
+
+def test_oracle_residue_nm1_when_3_divides_N(oracle_mod):
+    """base^(N-1) is computed correctly also when gcd(base, N) > 1 (reference src/prp.c:63-144)"""
+    lib = oracle_mod.load()
+    for k, n in [(5, 100), (11, 64), (13, 96), (7, 200), (1, 127)]:
+        N = k * (1 << n) - 1
+        nl = (n + 127) // 64
+        y = pow(3, N + 1, N)
+        arr = (C.c_uint64 * nl)(*[(y >> (64 * i)) & (2**64 - 1) for i in range(nl)])
+        Nl = (C.c_uint64 * nl)(*[(N >> (64 * i)) & (2**64 - 1) for i in range(nl)])
+        assert lib.ko_residue_nm1(arr, Nl, nl, 3) == 0
+        got = sum(int(arr[i]) << (64 * i) for i in range(nl))
+        assert got == pow(3, N - 1, N), (k, n)
+
+
+def _chains():
+    p = os.path.join(HERE, "golden", "chains.json")
+    if not os.path.exists(p):
+        return []
+    with open(p) as f:
+        return json.load(f)
+
+
+def _seeded_residue(seed, k, n):
+    import numpy as np
+    N = k * (1 << n) - 1
+    rng = np.random.Generator(np.random.PCG64(seed))
+    words = rng.integers(0, 2**64, size=(n + 127) // 64, dtype=np.uint64)
+    return int.from_bytes(words.astype("<u8").tobytes(), "little") % N
+
+
+@pytest.mark.parametrize("name", ["cpu_small", "cpu_mid"])
+def test_oracle_matches_gmp_fixture(oracle_mod, name):
+    ch = {c["name"]: c for c in _chains()}
+    if name not in ch:
+        pytest.skip("tests/golden/chains.json not generated")
+    c = ch[name]
+    k, n = c["k"], c["n"]
+    x0 = _seeded_residue(c["x0_seed"], k, n)
+    with oracle_mod.OracleCtx(k, n, 0) as o:
+        x = o.num(x0)
+        o.square(x, c["squarings"])
+        v = o.get(x)
+        nl = (n + 127) // 64
+        assert hashlib.sha256(v.to_bytes(8 * nl, "little")).hexdigest() == c["sha256_limbs"]
+        assert o.maxerr() < 0.4
+
+
+# ---- against the reference's own portable backends (built here from its sources) -------------
+
+def _ref_lib():
+    from oracle import oracle
+    if not os.path.exists(oracle.REF_LIB):
+        if not os.path.isdir(os.path.join(oracle.REFERENCE_SRC, "src")):
+            pytest.skip("reference sources not present (GPU box): compared in the build container")
+        oracle.build(ref=True)
+    lib = C.CDLL(oracle.REF_LIB)
+    lib.kite_ctx_new.restype = C.c_void_p
+    lib.kite_ctx_new.argtypes = [C.c_uint64, C.c_uint64, C.c_int32, C.c_void_p]
+    lib.kite_ctx_free.argtypes = [C.c_void_p]
+    lib.kite_num_new.restype = C.c_void_p
+    lib.kite_num_new.argtypes = [C.c_void_p]
+    lib.kite_num_free.argtypes = [C.c_void_p, C.c_void_p]
+    lib.kite_set_limbs.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]
+    lib.kite_get_limbs.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]
+    lib.kite_square_n.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64]
+    lib.kite_limbs.restype = C.c_size_t
+    lib.kite_limbs.argtypes = [C.c_void_p]
+    lib.kite_fft_len.restype = C.c_uint32
+    lib.kite_fft_len.argtypes = [C.c_void_p]
+    return lib
+
+
+class _Opts(C.Structure):
+    _fields_ = [("backend", C.c_int), ("fft_len", C.c_uint32), ("threads", C.c_uint32),
+                ("plan_order", C.c_uint32)]
+
+
+@pytest.mark.parametrize("k,n,L", [(9357, 20000, 0), (1, 9941, 0), (4095, 30000, 1920)])
+def test_oracle_equals_reference_ref_backend(oracle_mod, k, n, L):
+    """same seeded input, 100 squarings: the oracle and the reference's `ref` backend agree"""
+    ref = _ref_lib()
+    o = _Opts(1, L, 0, 0)  # KITE_BACKEND_REF
+    ctx = ref.kite_ctx_new(k, n, -1, C.byref(o))
+    assert ctx
+    try:
+        Lr = ref.kite_fft_len(ctx)
+        nl = ref.kite_limbs(ctx)
+        rng = random.Random(n)
+        N = k * (1 << n) - 1
+        a = rng.randrange(N)
+        x = ref.kite_num_new(ctx)
+        arr = (C.c_uint64 * nl)(*[(a >> (64 * i)) & (2**64 - 1) for i in range(nl)])
+        ref.kite_set_limbs(ctx, x, arr)
+        ref.kite_square_n(ctx, x, 100)
+        out = (C.c_uint64 * nl)()
+        ref.kite_get_limbs(ctx, x, out)
+        want = sum(int(out[i]) << (64 * i) for i in range(nl))
+        ref.kite_num_free(ctx, x)
+    finally:
+        ref.kite_ctx_free(ctx)
+    with oracle_mod.OracleCtx(k, n, Lr) as oc:
+        y = oc.num(a)
+        oc.square(y, 100)
+        assert oc.get(y) == want == pow(a, 1 << 100, N)
