@@ -65,7 +65,8 @@ struct TestDesc {
     // operands of the current operation
     double2 *x;
     const double2 *y;
-    int track_err;
+    int count;      // steps of the current launch sequence this test takes part in
+    int err_every;  // round-off is tracked on steps that are multiples of this
 };
 
 // A unit of work: the test and the row pair or column group it covers.

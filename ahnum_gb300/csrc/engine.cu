@@ -12,31 +12,39 @@
 #include "kernels.h"
 #include "layout.h"
 #include "plan.h"
+#include "engine_internal.h"
 
 using namespace kg;
 
-struct kc_engine {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    Layout lay;
-    std::shared_ptr<LengthPlan> plan;
-    TestDesc desc{};
-    TestDesc *d_desc = nullptr;
-    WorkItem *d_work = nullptr;  // rows then columns
-    LaunchSet ls;
-    uint8_t *d_bits = nullptr;
-    double *d_w = nullptr, *d_osc = nullptr, *d_idig = nullptr;
-    long long *d_dig = nullptr, *d_slot = nullptr;
-    unsigned long long *d_maxerr = nullptr;
-    int *d_status = nullptr;
-    long long *h_dig = nullptr;      // pinned staging for digit transfers
-    unsigned long long *h_err = nullptr;
-    int err = 0;
-    uint32_t err_every = 1;
-    uint64_t op_count = 0;
-    int add_cached = 0;              // constant currently folded in desc (0: none)
-    int64_t add_c = 0;
-};
+namespace {
+
+}  // namespace
+
+bool kc_ok(kc_engine *e, cudaError_t rc) {
+    if (rc != cudaSuccess && !e->err) e->err = -(int)rc;
+    return rc == cudaSuccess;
+}
+
+int kc_get_limbs(kc_engine *e, const double *x, uint64_t *limbs) {
+    std::vector<int64_t> d(e->lay.L);
+    if (kc_to_digits(e, x, d.data())) return e->err ? e->err : -1;
+    e->lay.digits_to_limbs(d.data(), limbs);
+    return 0;
+}
+
+int kc_set_limbs(kc_engine *e, double *x, const uint64_t *limbs) {
+    std::vector<int64_t> d(e->lay.L);
+    e->lay.limbs_to_digits(limbs, d.data());
+    return kc_from_digits(e, x, d.data());
+}
+
+int kc_mul_small_host(kc_engine *e, double *x, int64_t m) {
+    std::vector<int64_t> d(e->lay.L);
+    if (kc_to_digits(e, x, d.data())) return e->err ? e->err : -1;
+    for (auto &v : d) v *= m;
+    e->lay.carry(d.data());
+    return kc_from_digits(e, x, d.data());
+}
 
 namespace {
 
@@ -212,6 +220,8 @@ kc_engine *kc_engine_new(uint64_t k, uint64_t n, uint32_t L, const uint8_t *bits
         d.nadd = 0;
         d.x = nullptr;
         d.y = nullptr;
+        d.count = 1 << 30;
+        d.err_every = 1;
         good = upload_desc(e) && ok(e, cudaStreamSynchronize(e->stream));
         LaunchSet &s = e->ls;
         s.stream = e->stream;

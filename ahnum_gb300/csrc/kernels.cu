@@ -50,12 +50,15 @@ __device__ __forceinline__ void split_pair(double2 &a, double2 &b, double2 w, bo
 template <bool MUL>
 __global__ void __launch_bounds__(kThreads) k_rows(const TestDesc *__restrict__ tests,
                                                    const WorkItem *__restrict__ work, int nwork,
-                                                   double2 *xo, const double2 *yo) {
+                                                   const int *nwork_dev, int step, double2 *xo,
+                                                   const double2 *yo) {
     extern __shared__ double2 sm[];
     constexpr int ls = MUL ? 4 : 2;
+    if (nwork_dev) nwork = *nwork_dev;
     for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
         const WorkItem it = work[wi];
         const TestDesc &T = tests[it.test];
+        if (step >= T.count) continue;
         double2 *x = xo ? xo : T.x;
         const double2 *y = MUL ? (yo ? yo : T.y) : nullptr;
         const int C = T.C;
@@ -165,12 +168,16 @@ __device__ __forceinline__ void block_max_err(unsigned long long v, unsigned lon
 template <bool ERR>
 __global__ void __launch_bounds__(kThreads) k_col_inverse(const TestDesc *__restrict__ tests,
                                                           const WorkItem *__restrict__ work,
-                                                          int nwork, const double2 *xo) {
+                                                          int nwork, const int *nwork_dev,
+                                                          int step, const double2 *xo) {
     extern __shared__ double2 sm[];
     constexpr int G = kGroup;
+    if (nwork_dev) nwork = *nwork_dev;
     for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
         const WorkItem it = work[wi];
         const TestDesc &T = tests[it.test];
+        if (step >= T.count) continue;
+        const bool track = ERR && (step % T.err_every == 0);
         const double2 *x = xo ? xo : T.x;
         const int R = T.R, C = T.C, g = it.unit;
         for (int i = threadIdx.x; i < R * G; i += blockDim.x) {
@@ -190,7 +197,7 @@ __global__ void __launch_bounds__(kThreads) k_col_inverse(const TestDesc *__rest
                 const double2 z = sm[r * G + i / 2];
                 const double v = ((i & 1) ? z.y : z.x) * T.osc[j];
                 const double rv = rint(v);
-                if (ERR) {
+                if (ERR && track) {
                     const unsigned long long e = (unsigned long long)__double_as_longlong(fabs(v - rv));
                     emax = e > emax ? e : emax;
                 }
@@ -211,19 +218,22 @@ __global__ void __launch_bounds__(kThreads) k_col_inverse(const TestDesc *__rest
                 T.slot[g < T.NG - 1 ? (g + 1) * R + r : r + 1] = cy;
             }
         }
-        if (ERR) block_max_err(emax, T.maxerr);
+        if (ERR && track) block_max_err(emax, T.maxerr);
         __syncthreads();
     }
 }
 
 __global__ void __launch_bounds__(kThreads) k_col_forward(const TestDesc *__restrict__ tests,
                                                           const WorkItem *__restrict__ work,
-                                                          int nwork, double2 *xo, int use_slots) {
+                                                          int nwork, const int *nwork_dev, int step,
+                                                          double2 *xo, int use_slots) {
     extern __shared__ double2 sm[];
     constexpr int G = kGroup;
+    if (nwork_dev) nwork = *nwork_dev;
     for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
         const WorkItem it = work[wi];
         const TestDesc &T = tests[it.test];
+        if (step >= T.count) continue;
         double2 *x = xo ? xo : T.x;
         const int R = T.R, C = T.C, g = it.unit;
         for (int r = threadIdx.x; r < R; r += blockDim.x) {
@@ -316,19 +326,24 @@ int kernels_prepare(size_t row_smem, size_t col_smem) {
     return rc;
 }
 
-void launch_rows(const LaunchSet &s, bool mul, double2 *x, const double2 *y) {
+void launch_rows(const LaunchSet &s, bool mul, double2 *x, const double2 *y, int step) {
     const size_t smem = s.row_smem_per_lane * (mul ? 4 : 2);
-    if (mul) k_rows<true><<<s.grid_rows, kThreads, smem, s.stream>>>(s.tests, s.rows, s.nrows, x, y);
-    else k_rows<false><<<s.grid_rows, kThreads, smem, s.stream>>>(s.tests, s.rows, s.nrows, x, y);
+    if (mul)
+        k_rows<true><<<s.grid_rows, kThreads, smem, s.stream>>>(s.tests, s.rows, s.nrows, s.nrows_dev, step, x, y);
+    else
+        k_rows<false><<<s.grid_rows, kThreads, smem, s.stream>>>(s.tests, s.rows, s.nrows, s.nrows_dev, step, x, y);
 }
 
-void launch_col_inverse(const LaunchSet &s, bool err, const double2 *x) {
-    if (err) k_col_inverse<true><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, x);
-    else k_col_inverse<false><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, x);
+void launch_col_inverse(const LaunchSet &s, bool err, const double2 *x, int step) {
+    if (err)
+        k_col_inverse<true><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x);
+    else
+        k_col_inverse<false><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x);
 }
 
-void launch_col_forward(const LaunchSet &s, double2 *x, bool use_slots) {
-    k_col_forward<<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, x, use_slots ? 1 : 0);
+void launch_col_forward(const LaunchSet &s, double2 *x, bool use_slots, int step) {
+    k_col_forward<<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x,
+                                                                   use_slots ? 1 : 0);
 }
 
 void launch_col_digits(const LaunchSet &s, const double2 *x) {
@@ -339,6 +354,23 @@ void launch_elementwise(cudaStream_t st, double2 *x, const double2 *y, size_t n,
     int grid = (int)((n + 255) / 256);
     if (grid > 4096) grid = 4096;
     k_elementwise<<<grid, 256, 0, st>>>(x, y, n, op);
+}
+
+// Dependent DFMA chains: 8 independent chains per thread so the pipe, not latency, limits.
+__global__ void k_fp64_probe(double *out, int iters) {
+    double a0 = threadIdx.x * 1e-9, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3;
+    double a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6, a7 = a0 + 7;
+    const double m = 0.999999999, c = 1e-12;
+    for (int i = 0; i < iters; i++) {
+        a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
+        a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+    }
+    const double s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+    if (s > 1e300) out[0] = s;
+}
+
+void launch_fp64_probe(cudaStream_t st, int grid, int block, int iters, double *out) {
+    k_fp64_probe<<<grid, block, 0, st>>>(out, iters);
 }
 
 }  // namespace kg

@@ -18,6 +18,8 @@ struct LaunchSet {
     int nrows = 0;
     const WorkItem *cols = nullptr;    // device: column-group work items
     int ncols = 0;
+    const int *nrows_dev = nullptr;    // if set, the item counts are read on the device
+    const int *ncols_dev = nullptr;    //   (graphs captured once, lists refilled per launch)
     int grid_rows = 0, grid_cols = 0;
     size_t row_smem_per_lane = 0;      // C * sizeof(double2) for the longest row
     size_t col_smem = 0;               // R * kGroup * sizeof(double2) for the longest column
@@ -26,10 +28,14 @@ struct LaunchSet {
 // Raise the kernels' dynamic shared-memory limits; 0 on success.
 int kernels_prepare(size_t row_smem, size_t col_smem);
 
-// x, y non-null override the per-test operands (single-test use).
-void launch_rows(const LaunchSet &s, bool mul, double2 *x, const double2 *y);
-void launch_col_inverse(const LaunchSet &s, bool track_err, const double2 *x);
-void launch_col_forward(const LaunchSet &s, double2 *x, bool use_slots);
+// x, y non-null override the per-test operands (single-test use).  `step` is the index of
+// this squaring within a launch sequence: tests whose count is <= step sit it out.
+void launch_rows(const LaunchSet &s, bool mul, double2 *x, const double2 *y, int step = 0);
+void launch_col_inverse(const LaunchSet &s, bool track_err, const double2 *x, int step = 0);
+void launch_col_forward(const LaunchSet &s, double2 *x, bool use_slots, int step = 0);
+// FP64 FMA throughput probe: `iters` dependent-chain DFMAs per thread over grid x block;
+// the result is written to out[0] only if the chains overflow (never).
+void launch_fp64_probe(cudaStream_t st, int grid, int block, int iters, double *out);
 void launch_col_digits(const LaunchSet &s, const double2 *x);
 // op: 0 copy, 1 add, 2 sub
 void launch_elementwise(cudaStream_t st, double2 *x, const double2 *y, size_t n, int op);

@@ -200,3 +200,58 @@ def llr(k: int, n: int, fft_len: int = 0, inject_fault_at: int = 0, inject_fault
     rc = lib.kite_llr(k, n, C.byref(o), C.byref(r))
     return LlrResult(rc, bool(r.is_prime), r.factor, r.res64, r.P, r.fft_len, r.maxerr,
                      r.roundoff_retries, r.confirm_runs, r.seconds)
+
+
+class Batch:
+    """Many independent tests on one GPU (kc_batch_*): admit, step, collect."""
+
+    def __init__(self, gerbicz_block: int = 1000, gerbicz_blocks: int = 0, mem_budget: int = 0,
+                 device: int = -1):
+        self.lib = native.load()
+        self.h = self.lib.kc_batch_new(device, gerbicz_block, gerbicz_blocks, mem_budget)
+        if not self.h:
+            raise KiteError("kc_batch_new failed")
+        self.gpu_ms = 0.0
+
+    def close(self):
+        if self.h:
+            self.lib.kc_batch_free(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def add_fermat(self, k: int, n: int, base: int = 3, fft_len: int = 0) -> int:
+        return self.lib.kc_batch_add_fermat(self.h, k, n, base, fft_len)
+
+    def add_llr(self, k: int, n: int, fft_len: int = 0) -> int:
+        return self.lib.kc_batch_add_llr(self.h, k, n, fft_len)
+
+    def step(self, blocks: int = 1) -> int:
+        ms = C.c_double()
+        r = self.lib.kc_batch_step(self.h, blocks, C.byref(ms))
+        if r < 0:
+            raise KiteError(f"kc_batch_step failed: {r}")
+        self.gpu_ms += ms.value
+        return r
+
+    def result(self, slot: int):
+        """(state, result): state 0 running, 1 done, 2 failed."""
+        r = native.KcTestResult()
+        st = self.lib.kc_batch_result(self.h, slot, C.byref(r))
+        return st, r
+
+    def release(self, slot: int):
+        self.lib.kc_batch_release(self.h, slot)
+
+    def active(self) -> int:
+        return self.lib.kc_batch_active(self.h)
+
+    def run(self, max_blocks: int = 1 << 30) -> None:
+        blocks = 0
+        while self.active() and blocks < max_blocks:
+            self.step(1)
+            blocks += 1

@@ -64,7 +64,18 @@ class KiteLlrResult(C.Structure):
                 ("resumed", C.c_int), ("resumed_at", C.c_uint64), ("seconds", C.c_double)]
 
 
+class KcTestResult(C.Structure):
+    _fields_ = [("kind", C.c_int), ("rc", C.c_int), ("k", C.c_uint64), ("n", C.c_uint64),
+                ("res64", C.c_uint64), ("is_prp", C.c_int), ("fft_len", C.c_uint32),
+                ("maxerr", C.c_double), ("gerbicz_errors", C.c_uint32),
+                ("roundoff_retries", C.c_uint32), ("squarings", C.c_uint64),
+                ("seconds", C.c_double), ("P", C.c_uint32), ("factor", C.c_uint64),
+                ("iter", C.c_uint64)]
+
+
 KITE_BACKEND_CUDA = 5
+KC_TEST_FERMAT = 0
+KC_TEST_LLR = 1
 
 # name -> (restype, argtypes); every symbol declared in include/kite.h and include/kite_cuda.h
 PROTOTYPES = {
@@ -123,6 +134,21 @@ PROTOTYPES = {
     "kc_sync": (C.c_int, [vp]),
     "kc_stream": (vp, [vp]),
     "kc_shape": (None, [vp, u32p, u32p]),
+    "kc_batch_new": (vp, [C.c_int, C.c_uint32, C.c_uint32, C.c_size_t]),
+    "kc_batch_free": (None, [vp]),
+    "kc_batch_add_fermat": (C.c_int, [vp, C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32]),
+    "kc_batch_add_llr": (C.c_int, [vp, C.c_uint64, C.c_uint64, C.c_uint32]),
+    "kc_batch_step": (C.c_int, [vp, C.c_uint32, dp]),
+    "kc_batch_result": (C.c_int, [vp, C.c_int, C.POINTER(KcTestResult)]),
+    "kc_batch_release": (None, [vp, C.c_int]),
+    "kc_batch_active": (C.c_int, [vp]),
+    "kc_batch_bytes_in_use": (C.c_size_t, [vp]),
+    "kc_batch_budget": (C.c_size_t, [vp]),
+    "kc_batch_error": (C.c_int, [vp]),
+    "kc_fp64_peak": (C.c_double, [C.c_int]),
+    "kc_batch_profile": (C.c_int, [vp, C.c_uint32, dp, dp]),
+    "kc_batch_read": (C.c_int, [vp, C.c_int, u64p]),
+    "kc_batch_last_transfer": (None, [vp, u64p, u64p]),
     "kc_layout": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, u8p, dp, dp, u64p]),
     "kc_digits_to_limbs": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, i64p, u64p]),
     "kc_limbs_to_digits": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, u64p, i64p]),

@@ -1,0 +1,344 @@
+"""Benchmark: Fermat base-3 tests per hour, batched on one GB300 (and one-at-a-time for
+comparison), with the reference's CPU path timed on the host cores beside it.
+
+Workload (the batched configuration): 256 concurrent Fermat base-3 PRP tests of N = k*2^n - 1,
+k uniform odd in [3, 10^4], n uniform integer in [300000, 700000] (numpy PCG64, seed 3), each at
+the FFT length the reference's length chooser picks (16K-56K words).  Synthetic, seeded: the
+reference publishes no benchmark suite.
+
+A step is one Gerbicz block of every test: B = 1000 squarings of each test's x (one CUDA graph
+of 3000 kernels over all 256 tests) plus the block's product d <- d*x.  The check of every M = 250
+blocks (another B squarings and a product) is charged analytically, as a factor (1 + 1/M).
+Throughput is the steady state of a served batch whose slots are refilled with tests of the same
+distribution:  tests/hour = 3600 * slots * B / (T_block * (1 + 1/M) * mean(n)).
+
+  value     T_block from CUDA events around the work on the batch stream
+  e2e       the same through the C ABI with host buffers: wall-clock kc_batch_step calls (their
+            H2D slot tables and work lists, D2H round-off), plus per-test admission (H2D of
+            x0 and the tables) and read-back (D2H of the residue), amortised per test
+  roofline  the dominant kernel's algorithmic FP64 FLOPs per launch over its CUDA-event time,
+            against the FP64 FMA peak measured on this GPU by a DFMA kernel
+  cpu_baseline  the reference's arithmetic on the host: the CPU oracle's port of the
+            reference's `ref` backend (one test per core on all cores) over a bounded sample
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Under torchrun each rank runs its own independent batch (replicas; the tests do not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+SLOTS = 256
+BLOCK = 1000
+BLOCKS_PER_CHECK = 250
+SEED = 3
+WORKLOAD = "fermat-batch-256: k odd U[3,1e4], n U[300000,700000], base 3, B=1000, M=250"
+
+
+def workload(seed: int = SEED, count: int = SLOTS):
+    import numpy as np
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ks = rng.integers(1, 5000, size=count) * 2 + 1      # odd in [3, 9999]
+    ns = rng.integers(300000, 700001, size=count)
+    return [(int(k), int(n)) for k, n in zip(ks, ns)]
+
+
+def rank_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_sample(tests, threads: int, squarings: int):
+    """The oracle (a port of the reference's ref backend) on `threads` host cores: one test per
+    core, `squarings` squarings each; returns (tests/hour, seconds of CPU work, detail)."""
+    from oracle import oracle
+    oracle.build(ref=False)
+    sample = [(k, n, oracle.choose_fft_len(k, n)) for k, n in tests]
+    t0 = time.perf_counter()
+    us = oracle.time_squarings(sample, threads, squarings)
+    wall = time.perf_counter() - t0
+    per_test_s = [n * u * 1e-6 * (1 + 1 / BLOCKS_PER_CHECK + 2 / BLOCK) for (k, n, _), u in zip(sample, us)]
+    tph = threads * 3600.0 / statistics.mean(per_test_s)
+    return tph, wall * threads, {"tests": len(sample), "squarings_each": squarings,
+                                 "us_per_sq_mean": statistics.mean(us)}
+
+
+def run_reference(args):
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    tests = workload()
+    sample = tests[:threads]
+    # each step: one test per core, a bounded number of squarings each
+    for _ in range(args.warmup):
+        cpu_sample(sample, threads, 4)
+    vals, secs = [], []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        tph, work, det = cpu_sample(sample, threads, 16)
+        vals.append(tph)
+        secs.append(work)
+    wall = time.perf_counter() - t0
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": "fermat_tests_per_hour", "value": value,
+        "unit": "tests/hour", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": wall * 1e3 / max(args.steps, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64)",
+        "config": {"workload": WORKLOAD, "sample": f"{len(sample)} tests x 16 squarings per step"},
+        "cpu_baseline": {"value": value, "unit": "tests/hour", "cores": threads, "kind": "port",
+                         "sample": f"{len(sample)} tests (one per core) x 16 squarings per step, "
+                                   "extrapolated to full tests"},
+        "e2e": {"value": value, "unit": "tests/hour", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    rank, world, local = rank_info()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist = dist_mod
+        dist.init_process_group("gloo")
+    from ahnum_gb300.build import build_library
+    build_library()
+    from ahnum_gb300 import native
+    from ahnum_gb300.kite import Batch, Ctx
+    lib = native.load()
+    device = local
+    import ctypes as C
+
+    tests = workload(seed=SEED + rank)
+    mean_n = statistics.mean(n for _, n in tests)
+
+    # ---- admission (H2D of x0 digits and tables), timed for e2e
+    b = Batch(gerbicz_block=BLOCK, gerbicz_blocks=BLOCKS_PER_CHECK, device=device)
+    t0 = time.perf_counter()
+    slots = [b.add_fermat(k, n) for k, n in tests]
+    t_admit = time.perf_counter() - t0
+    assert all(s >= 0 for s in slots), "admission failed"
+    lengths = {}
+    for s in slots:
+        st, r = b.result(s)
+        lengths[r.fft_len] = lengths.get(r.fft_len, 0) + 1
+
+    # ---- warm-up blocks (graph capture, clocks)
+    for _ in range(args.warmup):
+        b.step(1)
+
+    # ---- timed region: K blocks, events on the batch stream, barrier + max over ranks
+    if dist:
+        dist.barrier()
+    gpu_ms = []
+    wall = []
+    with Clocks(device) as clk:
+        for _ in range(args.steps):
+            ms = C.c_double()
+            w0 = time.perf_counter()
+            r = lib.kc_batch_step(b.h, 1, C.byref(ms))
+            wall.append(time.perf_counter() - w0)
+            if r < 0:
+                raise RuntimeError(f"kc_batch_step failed {r}")
+            gpu_ms.append(ms.value)
+    if dist:
+        dist.barrier()
+    t_block = statistics.mean(gpu_ms) * 1e-3
+    t_block_wall = statistics.mean(wall)
+    if dist:
+        import torch
+        tt = torch.tensor([t_block, t_block_wall], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_block, t_block_wall = float(tt[0]), float(tt[1])
+
+    ovh = 1 + 1 / BLOCKS_PER_CHECK
+    per_rank = 3600.0 * SLOTS * BLOCK / (t_block * ovh * mean_n)
+    value = per_rank * world
+
+    h2d = C.c_uint64()
+    d2h = C.c_uint64()
+    lib.kc_batch_last_transfer(b.h, C.byref(h2d), C.byref(d2h))
+
+    # ---- read-back of every residue (D2H + exact host conversion), timed for e2e
+    t0 = time.perf_counter()
+    for (k, n), s in zip(tests, slots):
+        limbs = (C.c_uint64 * ((n + 127) // 64))()
+        if lib.kc_batch_read(b.h, s, limbs) != 0:
+            raise RuntimeError("kc_batch_read failed")
+    t_read = time.perf_counter() - t0
+    e2e_per_test = (t_admit + t_read) / SLOTS + mean_n * ovh * t_block_wall / (SLOTS * BLOCK)
+    e2e_value = 3600.0 / e2e_per_test * world
+
+    # ---- roofline of the dominant kernel (after the timed region, on the same stream)
+    ms3 = (C.c_double * 3)()
+    fl3 = (C.c_double * 3)()
+    rc = lib.kc_batch_profile(b.h, 5, ms3, fl3)
+    peak = lib.kc_fp64_peak(device)
+    names = ["k_rows (row FFT + split square)", "k_col_inverse (inverse column FFT + round + carry)",
+             "k_col_forward (carry-in + forward column FFT)"]
+    dom = max(range(3), key=lambda q: ms3[q])
+    achieved = fl3[dom] / (ms3[dom] * 1e-3) if ms3[dom] > 0 else 0.0
+    kernels = {names[q]: {"ms_per_launch": ms3[q], "gflop_per_launch": fl3[q] / 1e9,
+                          "tflops": fl3[q] / (ms3[q] * 1e-3) / 1e12 if ms3[q] else 0}
+               for q in range(3)}
+    b.close()
+
+    # ---- single-test GPU path on the same tests (one at a time), per distinct length
+    single = {}
+    for L in sorted(lengths):
+        k, n = next((k, n) for k, n in tests if _len(lib, k, n) == L)
+        with Ctx(k, n) as c:
+            x = c.num(3)
+            c.square(x, 20)
+            c.sync()
+            s0 = time.perf_counter()
+            c.square(x, 200)
+            c.sync()
+            single[L] = (time.perf_counter() - s0) / 200
+    single_s = [n * single[_len(lib, k, n)] * (1 + 1 / BLOCKS_PER_CHECK + 2 / BLOCK) for k, n in tests]
+    single_tph = 3600.0 / statistics.mean(single_s)
+    with Ctx(9001, 662695, 49152) as c:
+        x = c.num(3)
+        c.square(x, 50)
+        c.sync()
+        s0 = time.perf_counter()
+        c.square(x, 1000)
+        c.sync()
+        us_sq_49152 = (time.perf_counter() - s0) / 1000 * 1e6
+
+    cpu = None
+    if rank == 0:
+        threads = os.cpu_count() or 1
+        tph, work, det = cpu_sample(tests[:threads], threads, args.cpu_squarings)
+        cpu = {"value": tph, "unit": "tests/hour", "cores": threads, "kind": "port",
+               "sample": f"{det['tests']} of the 256 tests, one per core, {det['squarings_each']} "
+                         f"squarings each ({work:.1f} s of CPU work), extrapolated to full tests"}
+
+    if rank == 0:
+        line = {
+            "metric": "fermat_tests_per_hour", "value": value, "unit": "tests/hour",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_block * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64)",
+            "config": {"workload": WORKLOAD, "slots": SLOTS, "mean_n": mean_n,
+                       "fft_lengths": {str(k): v for k, v in sorted(lengths.items())},
+                       "l2": "inputs larger than L2 (~256 x 0.3 MB numbers + 0.6 MB tables per test)"},
+            "e2e": {"value": e2e_value, "unit": "tests/hour", "h2d_bytes_per_step": h2d.value,
+                    "d2h_bytes_per_step": d2h.value,
+                    "admission_s": t_admit, "readback_s": t_read, "block_wall_s": t_block_wall},
+            "gpu_launches": args.steps * (3 * BLOCK + 3),
+            "clocks": clk.summary(),
+            "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12,
+                         "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+                         "traffic": None, "kernel": names[dom],
+                         "peak_source": "measured: DFMA dependent-chain kernel on this GPU "
+                                        "(MEASURED_PEAKS.json has no FP64 figure)"},
+            "kernels": kernels,
+            "single_test": {"tests_per_hour": single_tph, "us_per_squaring_L49152": us_sq_49152,
+                            "us_per_squaring_by_L": {str(L): v * 1e6 for L, v in sorted(single.items())},
+                            "batched_over_single": value / world / single_tph},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+_len_cache = {}
+
+
+def _len(lib, k, n):
+    key = (k, n)
+    if key not in _len_cache:
+        _len_cache[key] = lib.kc_choose_fft_len(k, n)
+    return _len_cache[key]
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-squarings", type=int, default=300)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -72,6 +72,72 @@ void *kc_stream(kc_engine *e);
 /* Four-step shape chosen for the engine's length: H = R * C complex points. */
 void kc_shape(const kc_engine *e, uint32_t *R, uint32_t *C);
 
+/* ---- batched engine ------------------------------------------------------------------------
+ * Many independent tests advanced together on one GPU.  The reference's form of concurrent
+ * tests is one context per test on CPU threads (`kite throughput`, tools/kite.c:65-105); a batch
+ * replaces those contexts: each test is a slot with its own modulus and FFT length, and every
+ * kernel launch covers all slots.  Fermat slots run the Gerbicz-checked driver of
+ * src/prp.c:407-567 (block B, check every M blocks, rollback, longer FFT on round-off above
+ * 0.40, doubled tail); LLR slots run the doubling V <- V^2 - 2 of src/llr.c:395-406 after the
+ * Lucas ladder.  Results are bit-identical to a test run alone. */
+typedef struct kc_batch kc_batch;
+
+enum { KC_TEST_FERMAT = 0, KC_TEST_LLR = 1 };
+
+typedef struct {
+    int kind;                  /* KC_TEST_FERMAT or KC_TEST_LLR */
+    int rc;                    /* 0, or the kite_prp / kite_llr error code */
+    uint64_t k, n;
+    uint64_t res64;            /* Fermat: low word of base^(N-1); LLR: of V_{k 2^(n-1)} */
+    int is_prp;                /* Fermat: PRP; LLR: the final V is 0 (prime) */
+    uint32_t fft_len;
+    double maxerr;
+    uint32_t gerbicz_errors;
+    uint32_t roundoff_retries;
+    uint64_t squarings;        /* modular products done, checks and retries included */
+    double seconds;            /* admission to verdict */
+    uint32_t P;                /* LLR */
+    uint64_t factor;           /* LLR: small factor found while choosing P */
+    uint64_t iter;             /* last verified iteration */
+} kc_test_result;
+
+/* gerbicz_block 0: 1000; gerbicz_blocks 0: max(block/4, 8); mem_budget 0: 80% of free memory. */
+kc_batch *kc_batch_new(int device, uint32_t gerbicz_block, uint32_t gerbicz_blocks, size_t mem_budget);
+void kc_batch_free(kc_batch *b);
+/* Admit a test (fft_len 0: chosen as kite_ctx_new does).  Returns the slot id, -1 for an
+ * invalid test, -2 when the memory budget is full. */
+int kc_batch_add_fermat(kc_batch *b, uint64_t k, uint64_t n, uint32_t base, uint32_t fft_len);
+int kc_batch_add_llr(kc_batch *b, uint64_t k, uint64_t n, uint32_t fft_len);
+/* Advance every active slot by `blocks` Gerbicz blocks (B squarings each, plus the block's
+ * product or check).  *gpu_ms receives the CUDA-event time of the work.  Returns the number of
+ * slots still active, or a negative CUDA error. */
+int kc_batch_step(kc_batch *b, uint32_t blocks, double *gpu_ms);
+/* 0 running, 1 finished (result valid), 2 failed (rc set), -1 no such slot. */
+int kc_batch_result(const kc_batch *b, int slot, kc_test_result *out);
+/* Canonical limbs (kite_limbs words) of the slot's current x, read back from the device. */
+int kc_batch_read(kc_batch *b, int slot, uint64_t *limbs);
+/* Host<->device bytes moved by the last kc_batch_step (slot tables, work lists, round-off). */
+void kc_batch_last_transfer(const kc_batch *b, uint64_t *h2d, uint64_t *d2h);
+/* Free a slot's device memory (its number becomes reusable by later admissions). */
+void kc_batch_release(kc_batch *b, int slot);
+int kc_batch_active(const kc_batch *b);
+size_t kc_batch_bytes_in_use(const kc_batch *b);
+size_t kc_batch_budget(const kc_batch *b);
+int kc_batch_error(const kc_batch *b);
+
+/* Per-kernel timing of the batched squaring: copies each running Fermat slot's x into its
+ * scratch number t and squares t `squarings` times with the three pass kernels launched one by
+ * one, CUDA events around each (on the batch stream).  ms[0..2] receive the mean duration of one
+ * launch of the row pass, the column inverse pass and the column forward pass; flops[0..2] the
+ * algorithmic FP64 operations one launch of each performs over all slots (the per-squaring count
+ * F(L) = 5 L log2(L/2) + 24 L split as 10 H log2 C + 10 L, 5 H log2 R + 7 L, 5 H log2 R + 7 L).
+ * Only valid while no slot is in its check or tail (it uses t).  0 or a negative CUDA error. */
+int kc_batch_profile(kc_batch *b, uint32_t squarings, double *ms, double *flops);
+
+/* Measured FP64 FMA throughput of `device` in FLOP/s (2 per FMA), from a dependent-chain DFMA
+ * kernel timed with CUDA events: the roofline denominator of this FP64-bound path. */
+double kc_fp64_peak(int device);
+
 /* ---- host-only helpers (no GPU needed) ---------------------------------------------------
  * The exact integer layer the engine's callers use, exported so a host can check or reuse it:
  * kc_layout fills the digit layout of (k, n, L) as the reference's build_layout does
