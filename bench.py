@@ -255,6 +255,15 @@ def run_ours(args):
                for q in range(3)}
     b.close()
 
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"metric": "fermat_tests_per_hour", "value": value, "unit": "tests/hour",
+                              "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                              "ms_per_step": t_block * 1e3, "quick": True, "kernels": kernels}), flush=True)
+        if dist:
+            dist.destroy_process_group()
+        return
+
     # ---- single-test GPU path on the same tests (one at a time), per distinct length
     single = {}
     for L in sorted(lengths):
@@ -333,6 +342,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-squarings", type=int, default=300)
+    ap.add_argument("--quick", action="store_true",
+                    help="skip the single-test and CPU legs (for profiler runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
