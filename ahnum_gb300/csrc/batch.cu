@@ -419,7 +419,7 @@ bool ensure_graph(kc_batch *b, const kc_batch::Lists &l, size_t row_lane, size_t
     }
     row_lane = std::max(row_lane, b->graph_row_smem);
     col_smem = std::max(col_smem, b->graph_col_smem);
-    if (kernels_prepare(row_lane * 4, col_smem)) return false;
+    if (kernels_prepare(row_lane * 6, col_smem)) return false;
     LaunchSet s = launch_set(b, l, row_lane, col_smem);
     cudaGraph_t g;
     if (!bok(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal))) return false;
@@ -456,7 +456,7 @@ kc_batch *kc_batch_new(int device, uint32_t gerbicz_block, uint32_t gerbicz_bloc
     cudaMemGetInfo(&fr, &tot);
     b->budget = mem_budget ? mem_budget : fr / 10 * 8;
     cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, device);
-    b->grid = b->nsm * 3;
+    b->grid = b->nsm * kMinBlocks;
     if (!bok(b, cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) || !bok(b, cudaEventCreate(&b->ev0)) ||
         !bok(b, cudaEventCreate(&b->ev1))) {
         kc_batch_free(b);
@@ -746,7 +746,7 @@ int kc_batch_profile(kc_batch *b, uint32_t squarings, double *ms, double *flops)
     max_smem(b, row_lane, col_smem);
     row_lane = std::max(row_lane, b->graph_row_smem);
     col_smem = std::max(col_smem, b->graph_col_smem);
-    if (kernels_prepare(row_lane * 4, col_smem)) return -1;
+    if (kernels_prepare(row_lane * 6, col_smem)) return -1;
     if (!fill_lists(b, b->lists[1], sq)) return b->err ? b->err : -1;
     LaunchSet s = launch_set(b, b->lists[1], row_lane, col_smem);
     cudaEvent_t ev[4];

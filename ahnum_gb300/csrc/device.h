@@ -2,11 +2,13 @@
 //
 // One squaring of a number of L real words uses a complex transform of H = L/2 points arranged
 // four-step as R rows x C columns, element m = r*C + c (row-major):
-//   stored form  S[p][c] = (column DIF over r of u, times w_H^{c*k_r}), p = pos_R(k_r), where
-//                u_m = x_{2m} w_{2m} + i x_{2m+1} w_{2m+1} are the weighted digits;
-//   row pass     forward row DIF (C points), real-split square or product, inverse row DIT;
-//   column pass  conj twiddle, inverse column DIT, unweight/round/carry, reweight, forward
-//                column DIF, twiddle.
+//   stored form  S[k_r][c] = (column transform over r of u, times w_H^{c*k_r}), rows in natural
+//                frequency order, where u_m = x_{2m} w_{2m} + i x_{2m+1} w_{2m+1} are the
+//                weighted digits;
+//   row pass     forward row transform (C points), real-split square or product, inverse row
+//                transform;
+//   column pass  conj twiddle, inverse column transform, unweight/round/carry, reweight,
+//                forward column transform, twiddle.
 // This is the pass structure of the reference's two-pass backend (src/fast2p.c:1-19); the
 // kernels that implement it are written for the GPU.
 #pragma once
@@ -20,9 +22,12 @@ constexpr int kMaxStages = 12;
 constexpr int kGroup = 8;        // columns per column-pass work unit (16 digits per row segment)
 constexpr int kMaxAddend = 4;    // sparse constant digits folded into the normaliser
 
-// In-place mixed-radix DIF (forward) / DIT (inverse) of length n, unnormalised.
-// Stage i has radix rad[i] and span span[i] = n / (rad[0]*...*rad[i]); its twiddles
-// w_{rad[i]*span[i]}^{t*j} (t < rad, j < span) start at tw + off[i], index t*span + j.
+// In-place mixed-radix decimation-in-time transform of length n, unnormalised, input in the
+// digit-reversed order pos() of the plan.  Stage i has radix rad[i] and span
+// span[i] = n / (rad[0]*...*rad[i]); stages run from i = nst-1 (span 1) to 0.  Stage i's
+// twiddle records start at tw + off[i]: for each j < span, rad-1 double2 -- tangent form
+// {tau1, c1} (radix 2), {tau1, tau2}, {tau3, c1}, {c2, c3/c1} (radix 4), or the complex
+// twiddles w^{t*j}, t = 1..rad-1 (odd radices), of w = exp(-2 pi i / (rad*span)).
 struct FftPlan {
     int n = 0;
     int nst = 0;
@@ -38,13 +43,12 @@ struct TestDesc {
     FftPlan rp, cp;          // row plan (length C), column plan (length R)
     const double2 *twr;      // row stage twiddles
     const double2 *twc;      // column stage twiddles
-    const double2 *t4;       // [p][c] four-step twiddle w_H^{c * k_r(p)}
-    const double2 *sw;       // [p][q] real-split twiddle w_H^{k_r(p) + R * k_c(q)}
-    const int *part0;        // [q] partner column position in the row with k_r = 0
-    const int *part1;        // [q] partner column position for k_r != 0: pos(C-1-k_c(q))
-    const int2 *pairs;       // row pairs (p, p') with k_r(p') = R - k_r(p), p <= p'
+    const double2 *t4;       // [k_r][c] four-step twiddle w_H^{c * k_r}
+    const double2 *sw;       // [k_r][k_c] real-split twiddle w_H^{k_r + R * k_c}
+    const int *posr;         // [r] digit-reversed position of the column transform
+    const int *posc;         // [c] digit-reversed position of the row transform
+    const int2 *pairs;       // row pairs (k_r, (R - k_r) mod R), k_r <= its partner
     int npairs;
-    int prow0;               // position of row k_r = 0 (always 0)
     // per-modulus tables
     const uint8_t *bits;     // [L]
     const double *w;         // [L] weights

@@ -200,11 +200,10 @@ kc_engine *kc_engine_new(uint64_t k, uint64_t n, uint32_t L, const uint8_t *bits
         d.twc = P.twc;
         d.t4 = P.t4;
         d.sw = P.sw;
-        d.part0 = P.part0;
-        d.part1 = P.part1;
+        d.posr = P.dposr;
+        d.posc = P.dposc;
         d.pairs = P.dpairs;
         d.npairs = (int)P.pairs.size();
-        d.prow0 = 0;
         d.bits = e->d_bits;
         d.w = e->d_w;
         d.osc = e->d_osc;
@@ -234,7 +233,7 @@ kc_engine *kc_engine_new(uint64_t k, uint64_t n, uint32_t L, const uint8_t *bits
         s.grid_cols = s.ncols;
         s.row_smem_per_lane = (size_t)P.C * sizeof(double2);
         s.col_smem = (size_t)P.R * kGroup * sizeof(double2);
-        good = good && kernels_prepare(s.row_smem_per_lane * 4, s.col_smem) == 0;
+        good = good && kernels_prepare(s.row_smem_per_lane * 6, s.col_smem) == 0;
     }
     if (!good) {
         release(e);

@@ -1,5 +1,17 @@
-// Device building blocks: complex helpers, radix-2/3/4/5/7/8 butterflies and the in-place
-// shared-memory mixed-radix transform used by the row and column kernels.
+// Device building blocks: complex helpers, radix butterflies and the in-place shared-memory
+// mixed-radix transform used by the row and column kernels.
+//
+// Every transform here is decimation in time (twiddles on the inputs of each butterfly).  The
+// caller places element i at position pos(i) (the digit-reversed order of the plan), then the
+// stages run from the last plan stage (span 1, no twiddles) to the first; the output is in
+// natural order.  The forward transform uses exp(-2 pi i/n) and the inverse its conjugate;
+// both are unnormalised.
+//
+// GB300's FP64 pipe is the bottleneck of the whole path, so the radix-2 and radix-4 stages use
+// tangent-form twiddles: w_t = c_t (1 + i tau_t), x_t * (1 + i tau_t) costs 2 FMAs and the real
+// factors c_t are folded into the butterfly, whose adds become FMAs.  A radix-4 butterfly with its
+// three twiddles is 22 FP64 instructions instead of 28.  The odd radices (3, 5, 7) use plain
+// complex twiddles.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -18,6 +30,14 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 w) {
 __device__ __forceinline__ double2 cmulc(double2 a, double2 w) {
     return make_double2(fma(a.x, w.x, a.y * w.y), fma(a.y, w.x, -(a.x * w.y)));
 }
+// c * z + a (real c)
+__device__ __forceinline__ double2 cfma(double c, double2 z, double2 a) {
+    return make_double2(fma(c, z.x, a.x), fma(c, z.y, a.y));
+}
+// x * (1 + i tau)
+__device__ __forceinline__ double2 tan_rot(double2 x, double tau) {
+    return make_double2(fma(-tau, x.y, x.x), fma(tau, x.x, x.y));
+}
 
 // cos(2 pi r / P), sin(2 pi r / P) for the odd radices
 template <int P>
@@ -26,7 +46,7 @@ template <int P>
 __device__ __forceinline__ double sin2pi(int r);
 
 template <>
-__device__ __forceinline__ double cos2pi<3>(int r) { return -0.5; }
+__device__ __forceinline__ double cos2pi<3>(int) { return -0.5; }
 template <>
 __device__ __forceinline__ double sin2pi<3>(int r) { return r == 1 ? 0.86602540378443864676 : -0.86602540378443864676; }
 template <>
@@ -88,35 +108,6 @@ struct Dft<4, INV> {
     }
 };
 
-template <bool INV>
-struct Dft<8, INV> {
-    static __device__ __forceinline__ void run(double2 *x) {
-        double2 e[4] = {x[0], x[2], x[4], x[6]};
-        double2 o[4] = {x[1], x[3], x[5], x[7]};
-        Dft<4, INV>::run(e);
-        Dft<4, INV>::run(o);
-        const double h = 0.70710678118654752440;
-        double2 t1, t2, t3;
-        if (!INV) {
-            t1 = make_double2((o[1].x + o[1].y) * h, (o[1].y - o[1].x) * h);
-            t2 = make_double2(o[2].y, -o[2].x);
-            t3 = make_double2((o[3].y - o[3].x) * h, -(o[3].x + o[3].y) * h);
-        } else {
-            t1 = make_double2((o[1].x - o[1].y) * h, (o[1].x + o[1].y) * h);
-            t2 = make_double2(-o[2].y, o[2].x);
-            t3 = make_double2(-(o[3].x + o[3].y) * h, (o[3].x - o[3].y) * h);
-        }
-        x[0] = cadd(e[0], o[0]);
-        x[4] = csub(e[0], o[0]);
-        x[1] = cadd(e[1], t1);
-        x[5] = csub(e[1], t1);
-        x[2] = cadd(e[2], t2);
-        x[6] = csub(e[2], t2);
-        x[3] = cadd(e[3], t3);
-        x[7] = csub(e[3], t3);
-    }
-};
-
 // odd P: pair x_m with x_{P-m}; y_j = A_j -+ i Z_j, y_{P-j} = A_j +- i Z_j
 template <int P, bool INV>
 struct DftOdd {
@@ -166,11 +157,46 @@ struct Dft<5, INV> : DftOdd<5, INV> {};
 template <bool INV>
 struct Dft<7, INV> : DftOdd<7, INV> {};
 
-// One stage of the in-place transform over `nl` interleaved sequences; element e of sequence l
-// is at buf[e * ls + l].  Forward (DIF): butterfly, then output twiddles w_{P*span}^{t*j}.
-// Inverse (DIT): conjugate input twiddles, then the inverse butterfly.
+// Radix-2 DIT butterfly, twiddle record {tau1, c1}: w1 = c1 (1 + i tau1) (conj for INV).
+template <bool INV>
+__device__ __forceinline__ void dit2_tan(double2 *x, const double2 *rec) {
+    const double2 r = __ldg(rec);
+    const double2 z1 = tan_rot(x[1], INV ? -r.x : r.x);
+    const double2 x0 = x[0];
+    x[0] = cfma(r.y, z1, x0);
+    x[1] = cfma(-r.y, z1, x0);
+}
+
+// Radix-4 DIT butterfly, twiddle record {tau1, tau2}, {tau3, c1}, {c2, rho = c3/c1}:
+//   y0 = a + c1 e', y2 = a - c1 e', y1 = b -+ i c1 f', y3 = b +- i c1 f'
+// with z_t = x_t (1 + i tau_t), a = x0 + c2 z2, b = x0 - c2 z2, e' = z1 + rho z3, f' = z1 - rho z3.
+template <bool INV>
+__device__ __forceinline__ void dit4_tan(double2 *x, const double2 *rec) {
+    const double2 r0 = __ldg(rec), r1 = __ldg(rec + 1), r2 = __ldg(rec + 2);
+    const double s = INV ? -1.0 : 1.0;
+    const double2 z1 = tan_rot(x[1], s * r0.x);
+    const double2 z2 = tan_rot(x[2], s * r0.y);
+    const double2 z3 = tan_rot(x[3], s * r1.x);
+    const double c1 = r1.y, c2 = r2.x, rho = r2.y;
+    const double2 a = cfma(c2, z2, x[0]);
+    const double2 b = cfma(-c2, z2, x[0]);
+    const double2 e = cfma(rho, z3, z1);
+    const double2 f = cfma(-rho, z3, z1);
+    x[0] = cfma(c1, e, a);
+    x[2] = cfma(-c1, e, a);
+    if (!INV) {
+        x[1] = make_double2(fma(c1, f.y, b.x), fma(-c1, f.x, b.y));
+        x[3] = make_double2(fma(-c1, f.y, b.x), fma(c1, f.x, b.y));
+    } else {
+        x[1] = make_double2(fma(-c1, f.y, b.x), fma(c1, f.x, b.y));
+        x[3] = make_double2(fma(c1, f.y, b.x), fma(-c1, f.x, b.y));
+    }
+}
+
+// One DIT stage over `nl` interleaved sequences: element e of sequence l at buf[e * ls + l].
+// Twiddle records of this stage: (P-1) double2 per j.
 template <int P, bool INV>
-__device__ __forceinline__ void fft_stage(double2 *__restrict__ buf, int n, int span, int ls, int nl,
+__device__ __forceinline__ void dit_stage(double2 *__restrict__ buf, int n, int span, int ls, int nl,
                                           const double2 *__restrict__ tw) {
     const int total = (n / P) * nl;
     for (int i = threadIdx.x; i < total; i += blockDim.x) {
@@ -183,18 +209,21 @@ __device__ __forceinline__ void fft_stage(double2 *__restrict__ buf, int n, int 
         double2 x[P];
 #pragma unroll
         for (int t = 0; t < P; t++) x[t] = buf[base + t * stride];
-        if (!INV) {
-            Dft<P, false>::run(x);
-            if (j) {
-#pragma unroll
-                for (int t = 1; t < P; t++) x[t] = cmul(x[t], __ldg(&tw[t * span + j]));
-            }
+        // span 1 (every j = 0) takes the plain butterfly; other stages take the twiddled one for
+        // every j, j = 0 included with its unit record, so no warp runs both code paths
+        if (span == 1) {
+            Dft<P, INV>::run(x);
+        } else if (P == 4) {
+            dit4_tan<INV>(x, tw + j * 3);
+        } else if (P == 2) {
+            dit2_tan<INV>(x, tw + j);
         } else {
-            if (j) {
 #pragma unroll
-                for (int t = 1; t < P; t++) x[t] = cmulc(x[t], __ldg(&tw[t * span + j]));
+            for (int t = 1; t < P; t++) {
+                const double2 w = __ldg(&tw[j * (P - 1) + t - 1]);
+                x[t] = INV ? cmulc(x[t], w) : cmul(x[t], w);
             }
-            Dft<P, true>::run(x);
+            Dft<P, INV>::run(x);
         }
 #pragma unroll
         for (int t = 0; t < P; t++) buf[base + t * stride] = x[t];
@@ -202,33 +231,25 @@ __device__ __forceinline__ void fft_stage(double2 *__restrict__ buf, int n, int 
 }
 
 template <bool INV>
-__device__ __forceinline__ void fft_stage_dispatch(int p, double2 *buf, int n, int span, int ls, int nl,
+__device__ __forceinline__ void dit_stage_dispatch(int p, double2 *buf, int n, int span, int ls, int nl,
                                                    const double2 *tw) {
     switch (p) {
-    case 2: fft_stage<2, INV>(buf, n, span, ls, nl, tw); break;
-    case 3: fft_stage<3, INV>(buf, n, span, ls, nl, tw); break;
-    case 4: fft_stage<4, INV>(buf, n, span, ls, nl, tw); break;
-    case 5: fft_stage<5, INV>(buf, n, span, ls, nl, tw); break;
-    case 7: fft_stage<7, INV>(buf, n, span, ls, nl, tw); break;
-    case 8: fft_stage<8, INV>(buf, n, span, ls, nl, tw); break;
+    case 2: dit_stage<2, INV>(buf, n, span, ls, nl, tw); break;
+    case 3: dit_stage<3, INV>(buf, n, span, ls, nl, tw); break;
+    case 4: dit_stage<4, INV>(buf, n, span, ls, nl, tw); break;
+    case 5: dit_stage<5, INV>(buf, n, span, ls, nl, tw); break;
+    case 7: dit_stage<7, INV>(buf, n, span, ls, nl, tw); break;
     default: break;
     }
 }
 
-// Whole transform; the caller synchronises before (data loaded) and this returns after a
-// final barrier.
+// Whole transform on data already placed in digit-reversed order (buf[pos(i)] = x_i); the
+// caller synchronises before, and this returns after a final barrier with natural order.
 template <bool INV>
 __device__ __forceinline__ void smem_fft(double2 *buf, const FftPlan &pl, const double2 *tw, int ls, int nl) {
-    if (!INV) {
-        for (int st = 0; st < pl.nst; st++) {
-            fft_stage_dispatch<false>(pl.rad[st], buf, pl.n, pl.span[st], ls, nl, tw + pl.off[st]);
-            __syncthreads();
-        }
-    } else {
-        for (int st = pl.nst - 1; st >= 0; st--) {
-            fft_stage_dispatch<true>(pl.rad[st], buf, pl.n, pl.span[st], ls, nl, tw + pl.off[st]);
-            __syncthreads();
-        }
+    for (int st = pl.nst - 1; st >= 0; st--) {
+        dit_stage_dispatch<INV>(pl.rad[st], buf, pl.n, pl.span[st], ls, nl, tw + pl.off[st]);
+        __syncthreads();
     }
 }
 

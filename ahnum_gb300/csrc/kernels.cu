@@ -48,10 +48,13 @@ __device__ __forceinline__ void split_pair(double2 &a, double2 &b, double2 w, bo
 }
 
 template <bool MUL>
-__global__ void __launch_bounds__(kThreads) k_rows(const TestDesc *__restrict__ tests,
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_rows(const TestDesc *__restrict__ tests,
                                                    const WorkItem *__restrict__ work, int nwork,
                                                    const int *nwork_dev, int step, double2 *xo,
                                                    const double2 *yo) {
+    // shared memory: A = rows to transform forward, ls lanes interleaved (x row k_r, x row
+    // R-k_r, and for a product the same rows of y); B = the split's output, 2 lanes, already in
+    // the digit-reversed order the inverse transform wants
     extern __shared__ double2 sm[];
     constexpr int ls = MUL ? 4 : 2;
     if (nwork_dev) nwork = *nwork_dev;
@@ -62,47 +65,51 @@ __global__ void __launch_bounds__(kThreads) k_rows(const TestDesc *__restrict__ 
         double2 *x = xo ? xo : T.x;
         const double2 *y = MUL ? (yo ? yo : T.y) : nullptr;
         const int C = T.C;
+        double2 *A = sm, *B = sm + (size_t)ls * C;
         const int2 pr = T.pairs[it.unit];
+        const bool self = pr.x == pr.y;
         const double2 *xa = x + (size_t)pr.x * C, *xb = x + (size_t)pr.y * C;
         for (int c = threadIdx.x; c < C; c += blockDim.x) {
-            sm[c * ls + 0] = xa[c];
-            sm[c * ls + 1] = xb[c];
+            const int p = __ldg(&T.posc[c]) * ls;
+            A[p + 0] = xa[c];
+            A[p + 1] = xb[c];
             if (MUL) {
-                sm[c * ls + 2] = y[(size_t)pr.x * C + c];
-                sm[c * ls + 3] = y[(size_t)pr.y * C + c];
+                A[p + 2] = y[(size_t)pr.x * C + c];
+                A[p + 3] = y[(size_t)pr.y * C + c];
             }
         }
         __syncthreads();
-        smem_fft<false>(sm, T.rp, T.twr, ls, ls);
+        smem_fft<false>(A, T.rp, T.twr, ls, self ? (MUL ? 3 : 1) : ls);
         const double2 *swp = T.sw + (size_t)pr.x * C;
         const double2 zero = make_double2(0, 0);
-        if (pr.x != pr.y) {
-            for (int q = threadIdx.x; q < C; q += blockDim.x) {
-                const int qb = T.part1[q];
-                double2 a = sm[q * ls], b = sm[qb * ls + 1];
-                double2 ya = MUL ? sm[q * ls + 2] : zero, yb = MUL ? sm[qb * ls + 3] : zero;
-                split_pair(a, b, swp[q], MUL, ya, yb);
-                sm[q * ls] = a;
-                sm[qb * ls + 1] = b;
+        if (!self) {
+            // U_k in row k_r pairs with U_{H-k} in row R-k_r, column C-1-k_c
+            for (int kc = threadIdx.x; kc < C; kc += blockDim.x) {
+                const int kb = C - 1 - kc;
+                double2 a = A[kc * ls], b = A[kb * ls + 1];
+                const double2 ya = MUL ? A[kc * ls + 2] : zero, yb = MUL ? A[kb * ls + 3] : zero;
+                split_pair(a, b, __ldg(&swp[kc]), MUL, ya, yb);
+                B[__ldg(&T.posc[kc]) * 2] = a;
+                B[__ldg(&T.posc[kb]) * 2 + 1] = b;
             }
         } else {
-            const int *part = pr.x == T.prow0 ? T.part0 : T.part1;
-            for (int q = threadIdx.x; q < C; q += blockDim.x) {
-                const int qb = part[q];
-                if (qb < q) continue;
-                double2 a = sm[q * ls], b = sm[qb * ls];
-                double2 ya = MUL ? sm[q * ls + 2] : zero, yb = MUL ? sm[qb * ls + 2] : zero;
-                split_pair(a, b, swp[q], MUL, ya, yb);
-                sm[q * ls] = a;
-                if (qb != q) sm[qb * ls] = b;
+            // rows 0 and R/2 pair with themselves: k_c with (C-k_c) mod C, resp. C-1-k_c
+            for (int kc = threadIdx.x; kc < C; kc += blockDim.x) {
+                const int kb = pr.x == 0 ? (C - kc) % C : C - 1 - kc;
+                if (kb < kc) continue;
+                double2 a = A[kc * ls], b = A[kb * ls];
+                const double2 ya = MUL ? A[kc * ls + 2] : zero, yb = MUL ? A[kb * ls + 2] : zero;
+                split_pair(a, b, __ldg(&swp[kc]), MUL, ya, yb);
+                B[__ldg(&T.posc[kc]) * 2] = a;
+                if (kb != kc) B[__ldg(&T.posc[kb]) * 2] = b;
             }
         }
         __syncthreads();
-        smem_fft<true>(sm, T.rp, T.twr, ls, 2);
+        smem_fft<true>(B, T.rp, T.twr, 2, self ? 1 : 2);
         double2 *oa = x + (size_t)pr.x * C, *ob = x + (size_t)pr.y * C;
         for (int c = threadIdx.x; c < C; c += blockDim.x) {
-            oa[c] = sm[c * ls + 0];
-            if (pr.x != pr.y) ob[c] = sm[c * ls + 1];
+            oa[c] = B[c * 2];
+            if (!self) ob[c] = B[c * 2 + 1];
         }
         __syncthreads();
     }
@@ -165,13 +172,30 @@ __device__ __forceinline__ void block_max_err(unsigned long long v, unsigned lon
     if ((threadIdx.x & 31) == 0 && v) atomicMax(dst, v);
 }
 
+// 1.5 * 2^52: for |v| < 2^51, fma(a, b, kMagic) rounds a*b to the nearest integer, which then
+// sits in the low bits of the result's encoding.
+constexpr double kMagic = 6755399441055744.0;
+constexpr long long kMagicBits = 0x4338000000000000ll;
+
+// load the group's columns times conj(w_H^{c k_r}) into digit-reversed rows of the buffer
+__device__ __forceinline__ void load_columns_conj(const TestDesc &T, const double2 *x, int g, double2 *sm) {
+    constexpr int G = kGroup;
+    const int C = T.C;
+    for (int i = threadIdx.x; i < T.R * G; i += blockDim.x) {
+        const int kr = i / G, l = i % G;
+        const size_t e = (size_t)kr * C + g * G + l;
+        sm[__ldg(&T.posr[kr]) * G + l] = cmulc(x[e], __ldg(&T.t4[e]));
+    }
+}
+
 template <bool ERR>
-__global__ void __launch_bounds__(kThreads) k_col_inverse(const TestDesc *__restrict__ tests,
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_inverse(const TestDesc *__restrict__ tests,
                                                           const WorkItem *__restrict__ work,
                                                           int nwork, const int *nwork_dev,
                                                           int step, const double2 *xo) {
     extern __shared__ double2 sm[];
     constexpr int G = kGroup;
+    long long *smd = reinterpret_cast<long long *>(sm);
     if (nwork_dev) nwork = *nwork_dev;
     for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
         const WorkItem it = work[wi];
@@ -180,34 +204,45 @@ __global__ void __launch_bounds__(kThreads) k_col_inverse(const TestDesc *__rest
         const bool track = ERR && (step % T.err_every == 0);
         const double2 *x = xo ? xo : T.x;
         const int R = T.R, C = T.C, g = it.unit;
-        for (int i = threadIdx.x; i < R * G; i += blockDim.x) {
-            const int p = i / G, c = g * G + i % G;
-            sm[i] = cmulc(x[(size_t)p * C + c], T.t4[(size_t)p * C + c]);
-        }
+        load_columns_conj(T, x, g, sm);
         __syncthreads();
         smem_fft<true>(sm, T.cp, T.twc, G, G);
+        // unweight, scale and round every value in parallel: one FMA with the magic constant
+        // (two more when the round-off is tracked); the integer is read from the encoding
         unsigned long long emax = 0;
+        for (int i = threadIdx.x; i < R * G; i += blockDim.x) {
+            const int r = i / G, l = i % G;
+            const int j = 2 * (r * C + g * G + l);
+            const double2 z = sm[i];
+            const double o0 = __ldg(&T.osc[j]), o1 = __ldg(&T.osc[j + 1]);
+            const double t0 = fma(z.x, o0, kMagic), t1 = fma(z.y, o1, kMagic);
+            const long long b0 = __double_as_longlong(t0), b1 = __double_as_longlong(t1);
+            if (((b0 >> 52) != 0x433) | ((b1 >> 52) != 0x433)) {
+                emax = 0x3FE0000000000000ull;  // |v| >= 2^51: report 0.5, the transform is too short
+            } else if (track) {
+                const unsigned long long e0 = __double_as_longlong(fabs(fma(z.x, o0, kMagic - t0)));
+                const unsigned long long e1 = __double_as_longlong(fabs(fma(z.y, o1, kMagic - t1)));
+                emax = max(emax, max(e0, e1));
+            }
+            smd[2 * i] = b0 - kMagicBits;
+            smd[2 * i + 1] = b1 - kMagicBits;
+        }
+        __syncthreads();
+        // balanced carry along each row segment (16 digits), constants added first; the carry-out
+        // goes to the next segment's slot, the last segment's into the top fold
         for (int r = threadIdx.x; r < R; r += blockDim.x) {
             const int j0 = 2 * (r * C + g * G);
             long long d[2 * G];
             long long cy = 0;
 #pragma unroll
             for (int i = 0; i < 2 * G; i++) {
-                const int j = j0 + i;
-                const double2 z = sm[r * G + i / 2];
-                const double v = ((i & 1) ? z.y : z.x) * T.osc[j];
-                const double rv = rint(v);
-                if (ERR && track) {
-                    const unsigned long long e = (unsigned long long)__double_as_longlong(fabs(v - rv));
-                    emax = e > emax ? e : emax;
-                }
-                long long xi = (long long)rv;
+                long long v = smd[2 * G * r + i];
                 for (int a = 0; a < T.nadd; a++)
-                    if (T.addj[a] == j) xi += T.addv[a];
-                xi += cy;
-                const int b = T.bits[j];
-                const long long q = (xi + (1ll << (b - 1))) >> b;
-                d[i] = xi - (q << b);
+                    if (T.addj[a] == j0 + i) v += T.addv[a];
+                v += cy;
+                const int b = __ldg(&T.bits[j0 + i]);
+                const long long q = (v + (1ll << (b - 1))) >> b;
+                d[i] = v - (q << b);
                 cy = q;
             }
 #pragma unroll
@@ -218,12 +253,12 @@ __global__ void __launch_bounds__(kThreads) k_col_inverse(const TestDesc *__rest
                 T.slot[g < T.NG - 1 ? (g + 1) * R + r : r + 1] = cy;
             }
         }
-        if (ERR && track) block_max_err(emax, T.maxerr);
+        block_max_err(emax, T.maxerr);  // every thread of the block reaches this
         __syncthreads();
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_col_forward(const TestDesc *__restrict__ tests,
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_forward(const TestDesc *__restrict__ tests,
                                                           const WorkItem *__restrict__ work,
                                                           int nwork, const int *nwork_dev, int step,
                                                           double2 *xo, int use_slots) {
@@ -236,6 +271,8 @@ __global__ void __launch_bounds__(kThreads) k_col_forward(const TestDesc *__rest
         if (step >= T.count) continue;
         double2 *x = xo ? xo : T.x;
         const int R = T.R, C = T.C, g = it.unit;
+        // absorb the carry-in into the segment's first digits (the last digit takes any rest),
+        // reweight, and place the row at its digit-reversed position
         for (int r = threadIdx.x; r < R; r += blockDim.x) {
             const int j0 = 2 * (r * C + g * G);
             long long d[2 * G];
@@ -245,7 +282,7 @@ __global__ void __launch_bounds__(kThreads) k_col_forward(const TestDesc *__rest
 #pragma unroll
             for (int i = 0; i < 2 * G - 1; i++) {
                 if (cy) {
-                    const int b = T.bits[j0 + i];
+                    const int b = __ldg(&T.bits[j0 + i]);
                     const long long v = d[i] + cy;
                     const long long q = (v + (1ll << (b - 1))) >> b;
                     d[i] = v - (q << b);
@@ -253,22 +290,24 @@ __global__ void __launch_bounds__(kThreads) k_col_forward(const TestDesc *__rest
                 }
             }
             d[2 * G - 1] += cy;
+            double2 *row = sm + __ldg(&T.posr[r]) * G;
 #pragma unroll
             for (int l = 0; l < G; l++)
-                sm[r * G + l] = make_double2((double)d[2 * l] * T.w[j0 + 2 * l],
-                                             (double)d[2 * l + 1] * T.w[j0 + 2 * l + 1]);
+                row[l] = make_double2((double)d[2 * l] * __ldg(&T.w[j0 + 2 * l]),
+                                      (double)d[2 * l + 1] * __ldg(&T.w[j0 + 2 * l + 1]));
         }
         __syncthreads();
         smem_fft<false>(sm, T.cp, T.twc, G, G);
         for (int i = threadIdx.x; i < R * G; i += blockDim.x) {
-            const int p = i / G, c = g * G + i % G;
-            x[(size_t)p * C + c] = cmul(sm[i], T.t4[(size_t)p * C + c]);
+            const int kr = i / G, l = i % G;
+            const size_t e = (size_t)kr * C + g * G + l;
+            x[e] = cmul(sm[i], __ldg(&T.t4[e]));
         }
         __syncthreads();
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_col_digits(const TestDesc *__restrict__ tests,
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_digits(const TestDesc *__restrict__ tests,
                                                          const WorkItem *__restrict__ work,
                                                          int nwork, const double2 *xo) {
     extern __shared__ double2 sm[];
@@ -278,10 +317,7 @@ __global__ void __launch_bounds__(kThreads) k_col_digits(const TestDesc *__restr
         const TestDesc &T = tests[it.test];
         const double2 *x = xo ? xo : T.x;
         const int R = T.R, C = T.C, g = it.unit;
-        for (int i = threadIdx.x; i < R * G; i += blockDim.x) {
-            const int p = i / G, c = g * G + i % G;
-            sm[i] = cmulc(x[(size_t)p * C + c], T.t4[(size_t)p * C + c]);
-        }
+        load_columns_conj(T, x, g, sm);
         __syncthreads();
         smem_fft<true>(sm, T.cp, T.twc, G, G);
         for (int i = threadIdx.x; i < R * G; i += blockDim.x) {
@@ -327,7 +363,7 @@ int kernels_prepare(size_t row_smem, size_t col_smem) {
 }
 
 void launch_rows(const LaunchSet &s, bool mul, double2 *x, const double2 *y, int step) {
-    const size_t smem = s.row_smem_per_lane * (mul ? 4 : 2);
+    const size_t smem = s.row_smem_per_lane * (mul ? 6 : 4);
     if (mul)
         k_rows<true><<<s.grid_rows, kThreads, smem, s.stream>>>(s.tests, s.rows, s.nrows, s.nrows_dev, step, x, y);
     else

@@ -8,6 +8,7 @@
 namespace kg {
 
 constexpr int kThreads = 256;
+constexpr int kMinBlocks = 4;  // CTAs per SM the pass kernels are compiled for (64 registers)
 
 // Everything one launch of the pass kernels needs: the test table, the work lists and the
 // grid sizes.  The same set serves a single test and a batch.

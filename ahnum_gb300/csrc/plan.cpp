@@ -19,8 +19,8 @@ LengthPlan::~LengthPlan() {
     cudaFree(twc);
     cudaFree(t4);
     cudaFree(sw);
-    cudaFree(part0);
-    cudaFree(part1);
+    cudaFree(dposr);
+    cudaFree(dposc);
     cudaFree(dpairs);
     if (prev >= 0) cudaSetDevice(prev);
 }
@@ -52,6 +52,9 @@ bool choose_shape(uint32_t H, uint32_t &R, uint32_t &C) {
 }
 
 bool make_fft_plan(int n, FftPlan &pl) {
+    // radix 4 throughout the power-of-two part (tangent twiddles), one radix 2 if needed, and
+    // the odd radices last: the last plan stage has span 1 and runs without twiddles, so the
+    // costlier odd butterflies take no twiddle multiplications there.
     pl = FftPlan{};
     pl.n = n;
     int m = n, st = 0;
@@ -61,9 +64,10 @@ bool make_fft_plan(int n, FftPlan &pl) {
         m /= p;
         return true;
     };
-    while (m % 8 == 0 && m > 8)
-        if (!push(8)) return false;
-    for (int p : {8, 4, 2, 3, 5, 7})
+    while (m % 4 == 0)
+        if (!push(4)) return false;
+    if (m % 2 == 0 && !push(2)) return false;
+    for (int p : {3, 5, 7})
         while (m % p == 0)
             if (!push(p)) return false;
     if (m != 1) return false;
@@ -73,7 +77,7 @@ bool make_fft_plan(int n, FftPlan &pl) {
         span /= pl.rad[i];
         pl.span[i] = span;
         pl.off[i] = off;
-        off += pl.rad[i] * span;
+        off += (pl.rad[i] - 1) * span;
     }
     return true;
 }
@@ -119,19 +123,42 @@ static void positions(const FftPlan &pl, std::vector<int> &rev, std::vector<int>
     }
 }
 
+// Twiddle records of every stage (see FftPlan): tangent form for radix 2 and 4, complex
+// twiddles for the odd radices.  A cosine that is exactly 0 is replaced by 2^-60 (and the
+// tangent scaled to match), which changes the product by far less than one ulp.
 static void stage_twiddles(const FftPlan &pl, std::vector<double2> &tw) {
     tw.clear();
+    const double tiny = std::ldexp(1.0, -60);
     for (int i = 0; i < pl.nst; i++) {
-        int p = pl.rad[i], s = pl.span[i], sz = p * s;
-        for (int t = 0; t < p; t++)
-            for (int j = 0; j < s; j++) tw.push_back(cis_neg((uint64_t)t * j, (uint64_t)sz));
+        const int p = pl.rad[i], s = pl.span[i], sz = p * s;
+        for (int j = 0; j < s; j++) {
+            double c[4] = {1, 1, 1, 1}, tau[4] = {0, 0, 0, 0};
+            double2 w[8];
+            for (int t = 1; t < p; t++) {
+                w[t] = cis_neg((uint64_t)t * j, (uint64_t)sz);
+                double cc = w[t].x;
+                if (cc == 0.0) cc = tiny;
+                if (t < 4) {
+                    c[t] = cc;
+                    tau[t] = w[t].y / cc;
+                }
+            }
+            if (p == 2) {
+                tw.push_back(make_double2(tau[1], c[1]));
+            } else if (p == 4) {
+                tw.push_back(make_double2(tau[1], tau[2]));
+                tw.push_back(make_double2(tau[3], c[1]));
+                tw.push_back(make_double2(c[2], c[3] / c[1]));
+            } else {
+                for (int t = 1; t < p; t++) tw.push_back(w[t]);
+            }
+        }
     }
 }
 
 std::shared_ptr<LengthPlan> build_plan_host(uint32_t L, std::vector<double2> *twr,
                                             std::vector<double2> *twc, std::vector<double2> *t4,
-                                            std::vector<double2> *sw, std::vector<int> *part0,
-                                            std::vector<int> *part1) {
+                                            std::vector<double2> *sw) {
     if (L % (2 * kGroup) || L < 64) return nullptr;
     auto pl = std::make_shared<LengthPlan>();
     pl->L = L;
@@ -142,33 +169,22 @@ std::shared_ptr<LengthPlan> build_plan_host(uint32_t L, std::vector<double2> *tw
     positions(pl->rp, pl->rev_c, pl->pos_c);
     positions(pl->cp, pl->rev_r, pl->pos_r);
     const uint32_t R = pl->R, C = pl->C, H = pl->H;
-    for (uint32_t p = 0; p < R; p++) {
-        int kr = pl->rev_r[p];
-        int p2 = pl->pos_r[(R - kr) % R];
-        if ((int)p <= p2) pl->pairs.push_back(make_int2((int)p, p2));
+    for (uint32_t kr = 0; kr < R; kr++) {
+        uint32_t k2 = (R - kr) % R;
+        if (kr <= k2) pl->pairs.push_back(make_int2((int)kr, (int)k2));
     }
     if (twr) stage_twiddles(pl->rp, *twr);
     if (twc) stage_twiddles(pl->cp, *twc);
     if (t4) {
         t4->resize((size_t)R * C);
-        for (uint32_t p = 0; p < R; p++)
-            for (uint32_t c = 0; c < C; c++)
-                (*t4)[(size_t)p * C + c] = cis_neg((uint64_t)c * pl->rev_r[p] % H, H);
+        for (uint32_t kr = 0; kr < R; kr++)
+            for (uint32_t c = 0; c < C; c++) (*t4)[(size_t)kr * C + c] = cis_neg((uint64_t)c * kr % H, H);
     }
     if (sw) {
         sw->resize((size_t)R * C);
-        for (uint32_t p = 0; p < R; p++)
-            for (uint32_t q = 0; q < C; q++)
-                (*sw)[(size_t)p * C + q] =
-                    cis_neg(((uint64_t)pl->rev_r[p] + (uint64_t)R * pl->rev_c[q]) % H, H);
-    }
-    if (part0) {
-        part0->resize(C);
-        for (uint32_t q = 0; q < C; q++) (*part0)[q] = pl->pos_c[(C - pl->rev_c[q]) % C];
-    }
-    if (part1) {
-        part1->resize(C);
-        for (uint32_t q = 0; q < C; q++) (*part1)[q] = pl->pos_c[C - 1 - pl->rev_c[q]];
+        for (uint32_t kr = 0; kr < R; kr++)
+            for (uint32_t kc = 0; kc < C; kc++)
+                (*sw)[(size_t)kr * C + kc] = cis_neg(((uint64_t)kr + (uint64_t)R * kc) % H, H);
     }
     return pl;
 }
@@ -190,13 +206,12 @@ std::shared_ptr<LengthPlan> get_plan(uint32_t L) {
     auto it = cache.find({dev, L});
     if (it != cache.end()) return it->second;
     std::vector<double2> twr, twc, t4, sw;
-    std::vector<int> p0, p1;
-    auto pl = build_plan_host(L, &twr, &twc, &t4, &sw, &p0, &p1);
+    auto pl = build_plan_host(L, &twr, &twc, &t4, &sw);
     if (!pl) return nullptr;
     pl->device = dev;
     bool ok = upload(twr, &pl->twr, pl->device_bytes) && upload(twc, &pl->twc, pl->device_bytes) &&
               upload(t4, &pl->t4, pl->device_bytes) && upload(sw, &pl->sw, pl->device_bytes) &&
-              upload(p0, &pl->part0, pl->device_bytes) && upload(p1, &pl->part1, pl->device_bytes) &&
+              upload(pl->pos_r, &pl->dposr, pl->device_bytes) && upload(pl->pos_c, &pl->dposc, pl->device_bytes) &&
               upload(pl->pairs, &pl->dpairs, pl->device_bytes);
     if (!ok) return nullptr;
     cache[{dev, L}] = pl;

@@ -19,7 +19,7 @@ struct LengthPlan {
     // device copies
     int device = -1;
     double2 *twr = nullptr, *twc = nullptr, *t4 = nullptr, *sw = nullptr;
-    int *part0 = nullptr, *part1 = nullptr;
+    int *dposr = nullptr, *dposc = nullptr;
     int2 *dpairs = nullptr;
     size_t device_bytes = 0;
     ~LengthPlan();
@@ -36,10 +36,9 @@ double2 cis_neg(uint64_t j, uint64_t m);
 // Cached plan for (current device, L); nullptr if L cannot be planned or the device upload
 // fails.  Thread-safe.
 std::shared_ptr<LengthPlan> get_plan(uint32_t L);
-// Host tables only (no device upload): used by host-side tests of the plan logic.
+// Host tables only (no device upload).
 std::shared_ptr<LengthPlan> build_plan_host(uint32_t L, std::vector<double2> *twr,
                                             std::vector<double2> *twc, std::vector<double2> *t4,
-                                            std::vector<double2> *sw, std::vector<int> *part0,
-                                            std::vector<int> *part1);
+                                            std::vector<double2> *sw);
 
 }  // namespace kg
