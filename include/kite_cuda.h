@@ -72,6 +72,25 @@ void *kc_stream(kc_engine *e);
 /* Four-step shape chosen for the engine's length: H = R * C complex points. */
 void kc_shape(const kc_engine *e, uint32_t *R, uint32_t *C);
 
+/* ---- a squaring that allocates nothing ---------------------------------------------------
+ * No counterpart in the reference (its backends run on the host and never allocate device
+ * memory).  y = x^2 mod N (x == y allowed) on engine e, like kc_square(e, y, 1) after copying x
+ * to y, but calling no cudaMalloc, cudaFree or other allocating routine.  It is for callers that
+ * cannot allocate when they need the product: code running during a CUDA stream capture, a
+ * plugin whose host owns the device memory through its own pool, or a latency-bound loop that
+ * cannot afford the device synchronisation of an allocation.  Its scratch is one static device
+ * array of about 0.55 MB that every GPU loading this library reserves until the process exits.
+ *   - lengths above KC_NOALLOC_MAX_WORDS words are refused with KC_NOALLOC_TOO_LARGE;
+ *   - the first call on a device looks up the array's device address (cudaGetSymbolAddress)
+ *     with that device current: make that first call before any stream capture begins;
+ *   - all calls share the array, so calls that overlap on the GPU (different streams, engines
+ *     or threads) race and corrupt each other's result: serialise them;
+ *   - round-off is tracked on every call into the engine's kc_maxerr.
+ * Returns 0, KC_NOALLOC_TOO_LARGE, or a negative CUDA error (also recorded on e). */
+#define KC_NOALLOC_MAX_WORDS 65536
+#define KC_NOALLOC_TOO_LARGE (-2)
+int kc_square_noalloc(kc_engine *e, const double *x, double *y);
+
 /* ---- batched engine ------------------------------------------------------------------------
  * Many independent tests advanced together on one GPU.  The reference's form of concurrent
  * tests is one context per test on CPU threads (`kite throughput`, tools/kite.c:65-105); a batch
