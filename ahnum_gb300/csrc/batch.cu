@@ -26,6 +26,7 @@
 #include "../../include/kite.h"
 #include "../../include/kite_cuda.h"
 #include "engine_internal.h"
+#include "persist.h"
 
 using namespace kg;
 
@@ -87,6 +88,7 @@ struct kc_batch {
     int grid = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int err = 0;
+    const char *what = "";      // the step that failed, for kc_batch_error_string
     uint64_t h2d = 0, d2h = 0;  // bytes moved by the current / last step
 };
 
@@ -95,6 +97,12 @@ namespace {
 bool bok(kc_batch *b, cudaError_t rc) {
     if (rc != cudaSuccess && !b->err) b->err = -(int)rc;
     return rc == cudaSuccess;
+}
+
+// a failure that is not a CUDA error: remember which step, return -1
+int fail(kc_batch *b, const char *what) {
+    b->what = what;
+    return b->err ? b->err : -1;
 }
 
 void free_lists(kc_batch::Lists &l) {
@@ -419,7 +427,10 @@ bool ensure_graph(kc_batch *b, const kc_batch::Lists &l, size_t row_lane, size_t
     }
     row_lane = std::max(row_lane, b->graph_row_smem);
     col_smem = std::max(col_smem, b->graph_col_smem);
-    if (kernels_prepare(row_lane * 6, col_smem)) return false;
+    if (kernels_prepare(row_lane * 6, col_smem)) {
+        b->what = "raising the kernels' shared-memory limit";
+        return false;
+    }
     LaunchSet s = launch_set(b, l, row_lane, col_smem);
     cudaGraph_t g;
     if (!bok(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal))) return false;
@@ -564,10 +575,10 @@ int kc_batch_step(kc_batch *b, uint32_t blocks, double *gpu_ms) {
         max_smem(b, row_lane, col_smem);
         const int cap_before = b->lists[0].cap_tests + b->lists[0].cap_rows + b->lists[0].cap_cols;
         TestDesc *before = b->lists[0].d_desc;
-        if (!fill_lists(b, b->lists[0], sq)) return b->err ? b->err : -1;
+        if (!fill_lists(b, b->lists[0], sq)) return fail(b, "filling the squaring work lists");
         const bool moved = before != b->lists[0].d_desc ||
                            cap_before != b->lists[0].cap_tests + b->lists[0].cap_rows + b->lists[0].cap_cols;
-        if (!ensure_graph(b, b->lists[0], row_lane, col_smem, moved)) return b->err ? b->err : -1;
+        if (!ensure_graph(b, b->lists[0], row_lane, col_smem, moved)) return fail(b, *b->what ? b->what : "capturing the block graph");
         bok(b, cudaEventRecord(b->ev0, b->stream));
         bok(b, cudaGraphLaunch(b->graph, b->stream));
         // ---- end of block products: d <- d*x (after t <- d) for running Fermat slots,
@@ -583,7 +594,7 @@ int kc_batch_step(kc_batch *b, uint32_t blocks, double *gpu_ms) {
             }
         }
         if (!mu.empty()) {
-            if (!fill_lists(b, b->lists[1], mu)) return b->err ? b->err : -1;
+            if (!fill_lists(b, b->lists[1], mu)) return fail(b, "filling the product work lists");
             LaunchSet ms = launch_set(b, b->lists[1], b->graph_row_smem, b->graph_col_smem);
             launch_rows(ms, true, nullptr, nullptr, 0);
             launch_col_inverse(ms, true, nullptr, 0);
@@ -711,6 +722,28 @@ int kc_batch_read(kc_batch *b, int slot, uint64_t *limbs) {
     return kc_get_limbs(s.e, s.x, limbs);
 }
 
+int kc_batch_checkpoint(kc_batch *b, int slot, const char *path) {
+    if (!path || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].used || !b->slots[slot].e) return -1;
+    cudaSetDevice(b->device);
+    if (!bok(b, cudaStreamSynchronize(b->stream))) return -1;
+    Slot &s = b->slots[slot];
+    const size_t nl = s.e->lay.nlimbs;
+    std::vector<uint64_t> vx(nl), vd(nl);
+    if (kc_get_limbs(s.e, s.vx, vx.data())) return -1;
+    if (s.kind == KC_TEST_FERMAT) {
+        if (kc_get_limbs(s.e, s.vd, vd.data())) return -1;
+        return prp_checkpoint_write(path, s.k, s.n, s.base, s.vi, s.res.fft_len, vx, vd) ? 0 : -1;
+    }
+    LlrCheckpointHeader h{};
+    h.k = s.k;
+    h.n = s.n;
+    h.P = s.res.P;
+    h.iter = s.vi;
+    h.fft_len = s.res.fft_len;
+    h.run = 0;
+    return llr_checkpoint_write(path, h, vx) ? 0 : -1;
+}
+
 void kc_batch_last_transfer(const kc_batch *b, uint64_t *h2d, uint64_t *d2h) {
     if (h2d) *h2d = b->h2d;
     if (d2h) *d2h = b->d2h;
@@ -726,6 +759,11 @@ void kc_batch_release(kc_batch *b, int slot) {
 }
 
 int kc_batch_error(const kc_batch *b) { return b->err; }
+
+const char *kc_batch_error_string(const kc_batch *b) {
+    if (b->err) return cudaGetErrorString((cudaError_t)(-b->err));
+    return b->what;
+}
 
 int kc_batch_profile(kc_batch *b, uint32_t squarings, double *ms, double *flops) {
     cudaSetDevice(b->device);

@@ -14,6 +14,8 @@
 // tests with different lengths.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "fft_device.cuh"
 #include "kernels.h"
 
@@ -351,14 +353,28 @@ static int set_smem(const void *fn, size_t bytes) {
                : -1;
 }
 
+// The limit is a property of each kernel in the device's context, shared by every engine and
+// batch of the process, so it only ever grows: lowering it for a small length would make later
+// launches (or captured graphs) of a longer length fail.
 int kernels_prepare(size_t row_smem, size_t col_smem) {
+    static std::mutex mu;
+    static size_t row_hw[kMaxDevices] = {}, col_hw[kMaxDevices] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return -1;
+    std::lock_guard<std::mutex> lock(mu);
     int rc = 0;
-    rc |= set_smem((const void *)k_rows<false>, row_smem);
-    rc |= set_smem((const void *)k_rows<true>, row_smem);
-    rc |= set_smem((const void *)k_col_inverse<false>, col_smem);
-    rc |= set_smem((const void *)k_col_inverse<true>, col_smem);
-    rc |= set_smem((const void *)k_col_forward, col_smem);
-    rc |= set_smem((const void *)k_col_digits, col_smem);
+    if (row_smem > row_hw[dev]) {
+        rc |= set_smem((const void *)k_rows<false>, row_smem);
+        rc |= set_smem((const void *)k_rows<true>, row_smem);
+        if (!rc) row_hw[dev] = row_smem;
+    }
+    if (col_smem > col_hw[dev]) {
+        rc |= set_smem((const void *)k_col_inverse<false>, col_smem);
+        rc |= set_smem((const void *)k_col_inverse<true>, col_smem);
+        rc |= set_smem((const void *)k_col_forward, col_smem);
+        rc |= set_smem((const void *)k_col_digits, col_smem);
+        if (!rc) col_hw[dev] = col_smem;
+    }
     return rc;
 }
 

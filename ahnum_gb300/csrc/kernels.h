@@ -8,7 +8,8 @@
 namespace kg {
 
 constexpr int kThreads = 256;
-constexpr int kMinBlocks = 4;  // CTAs per SM the pass kernels are compiled for (64 registers)
+constexpr int kMinBlocks = 4;   // CTAs per SM the pass kernels are compiled for (64 registers)
+constexpr int kMaxDevices = 64;  // devices tracked by the per-device tables of this library
 
 // Everything one launch of the pass kernels needs: the test table, the work lists and the
 // grid sizes.  The same set serves a single test and a batch.
@@ -26,7 +27,8 @@ struct LaunchSet {
     size_t col_smem = 0;               // R * kGroup * sizeof(double2) for the longest column
 };
 
-// Raise the kernels' dynamic shared-memory limits; 0 on success.
+// Raise (never lower) the kernels' dynamic shared-memory limits on the current device; 0 on
+// success.
 int kernels_prepare(size_t row_smem, size_t col_smem);
 
 // x, y non-null override the per-test operands (single-test use).  `step` is the index of

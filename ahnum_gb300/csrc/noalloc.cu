@@ -32,8 +32,6 @@ constexpr size_t kDigBytes = (size_t)KC_NOALLOC_MAX_WORDS * sizeof(long long);
 constexpr size_t kSlotBytes = (size_t)KC_NOALLOC_MAX_WORDS / 2 / kGroup * sizeof(long long);
 constexpr size_t kScratchBytes = kDescBytes + kDigBytes + kSlotBytes;
 
-constexpr int kMaxDevices = 64;
-
 }  // namespace
 
 // The scratch itself: ~0.55 MB per device, shared by every call.

@@ -34,7 +34,8 @@ static bool factorable(uint32_t n) {
 bool choose_shape(uint32_t H, uint32_t &R, uint32_t &C) {
     double best = 1e30;
     R = C = 0;
-    for (uint32_t c = 16; c <= 4096 && c <= H / 2; c += kGroup) {
+    // rows up to 2048 points: a product's row pass holds 6 rows of C points in shared memory
+    for (uint32_t c = 16; c <= 2048 && c <= H / 2; c += kGroup) {
         if (H % c) continue;
         uint32_t r = H / c;
         if (r < 2 || r > 2048 || !factorable(r) || !factorable(c)) continue;

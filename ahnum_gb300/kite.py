@@ -234,7 +234,8 @@ class Batch:
         ms = C.c_double()
         r = self.lib.kc_batch_step(self.h, blocks, C.byref(ms))
         if r < 0:
-            raise KiteError(f"kc_batch_step failed: {r}")
+            why = self.lib.kc_batch_error_string(self.h) or b""
+            raise KiteError(f"kc_batch_step failed: {r} ({why.decode()})")
         self.gpu_ms += ms.value
         return r
 

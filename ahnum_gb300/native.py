@@ -146,9 +146,11 @@ PROTOTYPES = {
     "kc_batch_bytes_in_use": (C.c_size_t, [vp]),
     "kc_batch_budget": (C.c_size_t, [vp]),
     "kc_batch_error": (C.c_int, [vp]),
+    "kc_batch_error_string": (C.c_char_p, [vp]),
     "kc_fp64_peak": (C.c_double, [C.c_int]),
     "kc_batch_profile": (C.c_int, [vp, C.c_uint32, dp, dp]),
     "kc_batch_read": (C.c_int, [vp, C.c_int, u64p]),
+    "kc_batch_checkpoint": (C.c_int, [vp, C.c_int, C.c_char_p]),
     "kc_batch_last_transfer": (None, [vp, u64p, u64p]),
     "kc_layout": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, u8p, dp, dp, u64p]),
     "kc_digits_to_limbs": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, i64p, u64p]),

@@ -135,6 +135,10 @@ int kc_batch_step(kc_batch *b, uint32_t blocks, double *gpu_ms);
 int kc_batch_result(const kc_batch *b, int slot, kc_test_result *out);
 /* Canonical limbs (kite_limbs words) of the slot's current x, read back from the device. */
 int kc_batch_read(kc_batch *b, int slot, uint64_t *limbs);
+/* Write the slot's last verified state to `path` in the reference's checkpoint formats:
+ * KITECKP1 (x and d limbs, src/prp.c:158-192) for Fermat slots, KITELLR1 (V limbs, run 0,
+ * src/llr.c:106-121) for LLR slots.  0, or -1 on failure. */
+int kc_batch_checkpoint(kc_batch *b, int slot, const char *path);
 /* Host<->device bytes moved by the last kc_batch_step (slot tables, work lists, round-off). */
 void kc_batch_last_transfer(const kc_batch *b, uint64_t *h2d, uint64_t *d2h);
 /* Free a slot's device memory (its number becomes reusable by later admissions). */
@@ -143,6 +147,8 @@ int kc_batch_active(const kc_batch *b);
 size_t kc_batch_bytes_in_use(const kc_batch *b);
 size_t kc_batch_budget(const kc_batch *b);
 int kc_batch_error(const kc_batch *b);
+/* What the last failed kc_batch_step failed at ("" if nothing failed). */
+const char *kc_batch_error_string(const kc_batch *b);
 
 /* Per-kernel timing of the batched squaring: copies each running Fermat slot's x into its
  * scratch number t and squares t `squarings` times with the three pass kernels launched one by

@@ -10,7 +10,10 @@ are; the reference publishes no suite.  Outputs:
   fermat.json    RES64 (low 64 bits of 3^(N-1) mod N) of seeded full Fermat tests at the
                  single-test sizes n = 369717 and n = 662695, and of a seeded mixed batch.
 
-Usage:  python tests/golden/make_golden.py [chains|fermat|all]
+  chains_large.json  100-squaring chains at the large single-test size (n in [2e7, 2.5e7],
+                 k odd in [3, 255]).
+
+Usage:  python tests/golden/make_golden.py [chains|large|fermat|all]
 The full Fermat residues take minutes each (GMP mpz_powm, one process per test).
 """
 from __future__ import annotations
@@ -96,6 +99,13 @@ CHAINS = [
     ("mersenne_44497", 103, 1, 44497, 5000),
 ]
 
+# the large single-test regime: k seeded odd in [3, 255], n seeded in [2e7, 2.5e7]
+LARGE_CHAINS = [
+    # name, seed, squarings
+    ("large_a", 4, 100),
+    ("large_b", 5, 100),
+]
+
 FERMAT = [
     # name, seed, n
     ("config1_full", 1, 369717),
@@ -107,6 +117,24 @@ def _chain(item):
     name, seed, k, n, count = item
     if k is None:
         k = seeded_k(seed)
+    N = k * (1 << n) - 1
+    x0 = seeded_residue(seed + 1000, k, n)
+    v = gmp_powm(x0, 1 << count, N)
+    sha, low = limbs_digest(v, n)
+    return {"name": name, "seed": seed, "k": k, "n": n, "squarings": count,
+            "x0_seed": seed + 1000, "sha256_limbs": sha, "low64": low}
+
+
+def seeded_large(seed: int):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    k = int(rng.integers(1, 128)) * 2 + 1          # odd in [3, 255]
+    n = int(rng.integers(20_000_000, 25_000_001))
+    return k, n
+
+
+def _large_chain(item):
+    name, seed, count = item
+    k, n = seeded_large(seed)
     N = k * (1 << n) - 1
     x0 = seeded_residue(seed + 1000, k, n)
     v = gmp_powm(x0, 1 << count, N)
@@ -131,6 +159,11 @@ def main(what: str) -> None:
             with open(os.path.join(HERE, "chains.json"), "w") as f:
                 json.dump(out, f, indent=1)
             print("chains.json written")
+        if what in ("large", "all"):
+            out = list(ex.map(_large_chain, LARGE_CHAINS))
+            with open(os.path.join(HERE, "chains_large.json"), "w") as f:
+                json.dump(out, f, indent=1)
+            print("chains_large.json written")
         if what in ("fermat", "all"):
             out = list(ex.map(_fermat, FERMAT))
             with open(os.path.join(HERE, "fermat.json"), "w") as f:
