@@ -5,6 +5,8 @@
 
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 
 namespace kg {
 
@@ -35,6 +37,23 @@ static double length_cost(uint32_t L) {
 
 static bool length_usable(uint32_t L) { return L % 64 == 0 && fft_len_ok(L); }
 
+// Measured microseconds per squaring by FFT length, from the autotuner or a tuning file; used as
+// the reference uses its `kite tune` times (src/ctx.c:123-140).
+static std::mutex g_times_mu;
+static std::map<uint32_t, double> g_times;
+
+void set_tuned_time(uint32_t L, double us) {
+    std::lock_guard<std::mutex> lock(g_times_mu);
+    if (us > 0) g_times[L] = us;
+    else g_times.erase(L);
+}
+
+static double tuned_time(uint32_t L) {
+    std::lock_guard<std::mutex> lock(g_times_mu);
+    auto it = g_times.find(L);
+    return it == g_times.end() ? -1.0 : it->second;
+}
+
 uint32_t choose_fft_len(uint64_t k, uint64_t n) {
     if (n < 2048) {
         for (uint32_t L = 16; L <= n; L *= 2)
@@ -48,11 +67,16 @@ uint32_t choose_fft_len(uint64_t k, uint64_t n) {
             break;
         }
     if (!lo) return 0;
+    // among the usable lengths up to 30 % longer: the fastest measured one when every one of
+    // them has a measurement, else the cheapest by the heuristic
+    bool measured = true;
+    for (uint32_t L = lo; L <= lo + lo / 10 * 3; L += 64)
+        if (length_usable(L) && tuned_time(L) < 0) measured = false;
     uint32_t best = lo;
     double bc = HUGE_VAL;
     for (uint32_t L = lo; L <= lo + lo / 10 * 3; L += 64) {
         if (!length_usable(L)) continue;
-        double c = length_cost(L);
+        double c = measured ? tuned_time(L) : length_cost(L);
         if (c < bc) {
             bc = c;
             best = L;

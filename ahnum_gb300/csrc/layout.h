@@ -19,6 +19,8 @@ bool fft_len_ok(uint32_t L);
 double safe_bpw(uint32_t L, uint64_t k);
 uint32_t choose_fft_len(uint64_t k, uint64_t n);
 uint32_t next_fft_len(uint32_t L);
+// Record (us > 0) or forget the measured time per squaring of length L (autotuner results).
+void set_tuned_time(uint32_t L, double us);
 
 struct Layout {
     uint64_t k = 0, n = 0;

@@ -3,9 +3,14 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
+#include "../../include/kite_cuda.h"
+
 #include <cmath>
 #include <map>
 #include <mutex>
+#include <tuple>
 #include <utility>
 
 namespace kg {
@@ -31,18 +36,62 @@ static bool factorable(uint32_t n) {
     return n == 1;
 }
 
+static bool shape_usable(uint32_t H, uint32_t r, uint32_t c) {
+    return r >= 2 && r <= 1024 && c >= 16 && c <= 2048 && c % kGroup == 0 && (uint64_t)r * c == H &&
+           factorable(r) && factorable(c);
+}
+
+// Shapes chosen by the autotuner (or a tuning file), by FFT length L = 2H: R rows.
+static std::mutex g_shape_mu;
+static std::map<uint32_t, uint32_t> g_shape;
+
+bool set_shape_override(uint32_t L, uint32_t R) {
+    std::lock_guard<std::mutex> lock(g_shape_mu);
+    if (!R) {
+        g_shape.erase(L);
+        return true;
+    }
+    if (L % 2 || R == 0 || (L / 2) % R || !shape_usable(L / 2, R, L / 2 / R)) return false;
+    g_shape[L] = R;
+    return true;
+}
+
+int shape_candidates(uint32_t H, uint32_t *R, uint32_t *C, int max) {
+    int n = 0;
+    for (uint32_t c = 16; c <= 2048 && c <= H / 2 && n < max; c += kGroup) {
+        if (H % c || !shape_usable(H, H / c, c)) continue;
+        const double ratio = (double)c / (H / c);
+        if (ratio < 0.5 || ratio > 64) continue;  // far from balanced: never the fastest
+        R[n] = H / c;
+        C[n] = c;
+        n++;
+    }
+    return n;
+}
+
 bool choose_shape(uint32_t H, uint32_t &R, uint32_t &C) {
+    static std::once_flag env_once;
+    std::call_once(env_once, [] {
+        if (const char *p = std::getenv("KITE_GB300_TUNING")) kc_tuning_load(p);
+    });
+    {
+        std::lock_guard<std::mutex> lock(g_shape_mu);
+        auto it = g_shape.find(2 * H);
+        if (it != g_shape.end()) {
+            R = it->second;
+            C = H / R;
+            return true;
+        }
+    }
     double best = 1e30;
     R = C = 0;
     // rows up to 2048 points: a product's row pass holds 6 rows of C points in shared memory
     for (uint32_t c = 16; c <= 2048 && c <= H / 2; c += kGroup) {
         if (H % c) continue;
         uint32_t r = H / c;
-        if (r < 2 || r > 2048 || !factorable(r) || !factorable(c)) continue;
-        // rows about four times as long as columns; columns beyond 1024 points need more
-        // shared memory per group than a CTA should hold
+        if (!shape_usable(H, r, c)) continue;
+        // rows about four times as long as columns
         double cost = std::fabs(std::log2((double)r) - std::log2((double)c) + 2.0);
-        if (r > 1024) cost += 10;
         if (cost < best) {
             best = cost;
             R = r;
@@ -200,11 +249,13 @@ static bool upload(const std::vector<T> &h, T **d, size_t &bytes) {
 
 std::shared_ptr<LengthPlan> get_plan(uint32_t L) {
     static std::mutex mu;
-    static std::map<std::pair<int, uint32_t>, std::shared_ptr<LengthPlan>> cache;
+    static std::map<std::tuple<int, uint32_t, uint32_t>, std::shared_ptr<LengthPlan>> cache;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    uint32_t R = 0, C = 0;
+    if (L % 2 || !choose_shape(L / 2, R, C)) return nullptr;
     std::lock_guard<std::mutex> lock(mu);
-    auto it = cache.find({dev, L});
+    auto it = cache.find({dev, L, R});
     if (it != cache.end()) return it->second;
     std::vector<double2> twr, twc, t4, sw;
     auto pl = build_plan_host(L, &twr, &twc, &t4, &sw);
@@ -215,7 +266,7 @@ std::shared_ptr<LengthPlan> get_plan(uint32_t L) {
               upload(pl->pos_r, &pl->dposr, pl->device_bytes) && upload(pl->pos_c, &pl->dposc, pl->device_bytes) &&
               upload(pl->pairs, &pl->dpairs, pl->device_bytes);
     if (!ok) return nullptr;
-    cache[{dev, L}] = pl;
+    cache[{dev, L, R}] = pl;
     return pl;
 }
 

@@ -25,8 +25,13 @@ struct LengthPlan {
     ~LengthPlan();
 };
 
-// H = R*C with C a multiple of kGroup; false if no usable shape exists.
+// H = R*C with C a multiple of kGroup; the autotuned shape of this length if one was set, else
+// rows about four times as long as columns.  false if no usable shape exists.
 bool choose_shape(uint32_t H, uint32_t &R, uint32_t &C);
+// Use R rows for FFT length L from now on (R = 0: back to the default); false if unusable.
+bool set_shape_override(uint32_t L, uint32_t R);
+// Usable shapes of H = R*C near balance, at most `max`; returns the count.
+int shape_candidates(uint32_t H, uint32_t *R, uint32_t *C, int max);
 // Radices for a length-n transform in DIF order; false if n has a prime factor above 7.
 bool make_fft_plan(int n, FftPlan &pl);
 

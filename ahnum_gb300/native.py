@@ -152,6 +152,12 @@ PROTOTYPES = {
     "kc_batch_read": (C.c_int, [vp, C.c_int, u64p]),
     "kc_batch_checkpoint": (C.c_int, [vp, C.c_int, C.c_char_p]),
     "kc_batch_last_transfer": (None, [vp, u64p, u64p]),
+    "kc_set_fft_shape": (C.c_int, [C.c_uint32, C.c_uint32]),
+    "kc_set_fft_time": (None, [C.c_uint32, C.c_double]),
+    "kc_fft_shape_candidates": (C.c_int, [C.c_uint32, u32p, u32p, C.c_int]),
+    "kc_fft_shape": (C.c_int, [C.c_uint32, u32p, u32p]),
+    "kc_tuning_load": (C.c_int, [C.c_char_p]),
+    "kc_roundoff_probe": (C.c_double, [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint64]),
     "kc_layout": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, u8p, dp, dp, u64p]),
     "kc_digits_to_limbs": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, i64p, u64p]),
     "kc_limbs_to_digits": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, u64p, i64p]),

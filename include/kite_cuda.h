@@ -163,6 +163,27 @@ int kc_batch_profile(kc_batch *b, uint32_t squarings, double *ms, double *flops)
  * kernel timed with CUDA events: the roofline denominator of this FP64-bound path. */
 double kc_fp64_peak(int device);
 
+/* ---- per-length tuning (replaces `kite tune`, tools/kite.c:274-326 and src/ctx.c:35-92) ------
+ * The four-step shape H = R*C of each FFT length can be chosen by measurement instead of the
+ * default (rows about four times as long as columns).  A tuning file has lines "L us R C":
+ * the length, its measured microseconds per squaring (batched throughput), and the shape; the
+ * times also drive the length choice among the safe lengths within 30 %, as the reference's
+ * tuning file does.  Plans built before a change keep their shape. */
+/* Use R rows for length L (R = 0: back to the default).  0, or -1 if the shape is unusable. */
+int kc_set_fft_shape(uint32_t L, uint32_t R);
+/* Record the measured time of length L (us <= 0 forgets it). */
+void kc_set_fft_time(uint32_t L, double us);
+/* Candidate shapes of length L near balance: up to `max` (R, C) pairs; returns the count. */
+int kc_fft_shape_candidates(uint32_t L, uint32_t *R, uint32_t *C, int max);
+/* The shape length L gets now. 0, or -1. */
+int kc_fft_shape(uint32_t L, uint32_t *R, uint32_t *C);
+/* Load a tuning file (shapes and times).  Returns the number of lengths read, -1 if unreadable.
+ * The library also loads $KITE_GB300_TUNING, if set, when it plans its first length. */
+int kc_tuning_load(const char *path);
+/* Largest round-off of `squarings` squarings of a seeded residue mod k*2^n-1 at length L on the
+ * current GPU (the reference's tools/sweep_err.c measurement); negative on failure. */
+double kc_roundoff_probe(uint64_t k, uint64_t n, uint32_t L, uint32_t squarings, uint64_t seed);
+
 /* ---- host-only helpers (no GPU needed) ---------------------------------------------------
  * The exact integer layer the engine's callers use, exported so a host can check or reuse it:
  * kc_layout fills the digit layout of (k, n, L) as the reference's build_layout does
