@@ -213,7 +213,7 @@ bool power_start(Slot &s) {
 
 bool open_engine(kc_batch *b, Slot &s, uint32_t L) {
     cudaSetDevice(b->device);
-    s.e = kc_engine_new(s.k, s.n, L, nullptr, nullptr, nullptr, 0, 0, 0, 0, b->device);
+    s.e = kc_engine_create(s.k, s.n, L, nullptr, nullptr, nullptr, 0, 0, 0, 0, b->device, true);
     if (!s.e) return false;
     s.res.fft_len = L;
     return alloc_numbers(s);
@@ -380,7 +380,7 @@ bool fill_lists(kc_batch *b, kc_batch::Lists &l, const std::vector<Entry> &ents)
     int rows = 0, cols = 0;
     for (auto &en : ents) {
         rows += (int)en.s->e->plan->pairs.size();
-        cols += (int)en.s->e->plan->NG;
+        cols += (int)en.s->e->NG;
     }
     if (!grow_lists(b, l, (int)ents.size(), rows, cols)) return false;
     std::vector<std::pair<int, WorkItem>> rv, cv;
@@ -399,7 +399,7 @@ bool fill_lists(kc_batch *b, kc_batch::Lists &l, const std::vector<Entry> &ents)
         l.h_desc[t] = d;
         const LengthPlan &P = *en.s->e->plan;
         for (size_t p = 0; p < P.pairs.size(); p++) rv.push_back({(int)P.C, WorkItem{(int)t, (int)p}});
-        for (uint32_t g = 0; g < P.NG; g++) cv.push_back({(int)P.R, WorkItem{(int)t, (int)g}});
+        for (uint32_t g = 0; g < en.s->e->NG; g++) cv.push_back({(int)P.R, WorkItem{(int)t, (int)g}});
     }
     // longest items first, so the grid-stride walk ends with the short ones
     auto by_size = [](const std::pair<int, WorkItem> &a, const std::pair<int, WorkItem> &c) { return a.first > c.first; };

@@ -19,7 +19,7 @@
 namespace kg {
 
 constexpr int kMaxStages = 12;
-constexpr int kGroup = 8;        // columns per column-pass work unit (16 digits per row segment)
+constexpr int kGroup = 8;        // widest column group (16 digits per row segment); C is a multiple of it
 constexpr int kMaxAddend = 4;    // sparse constant digits folded into the normaliser
 
 // In-place mixed-radix decimation-in-time transform of length n, unnormalised, input in the
@@ -39,7 +39,8 @@ struct FftPlan {
 // Everything a kernel needs for one test (one modulus).  Lives in device memory.
 struct TestDesc {
     // shape
-    int L, H, R, C, NG;      // NG = C / kGroup column groups
+    int L, H, R, C, NG;      // NG = C / G column groups
+    int G;                   // columns per column group: 2, 4 or 8 (2G digits per row segment)
     FftPlan rp, cp;          // row plan (length C), column plan (length R)
     const double2 *twr;      // row stage twiddles
     const double2 *twc;      // column stage twiddles

@@ -74,6 +74,8 @@ bool dalloc(kc_engine *e, T **p, size_t count) {
 }
 
 void release(kc_engine *e) {
+    for (auto &g : e->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     cudaFree(e->d_desc);
     cudaFree(e->d_work);
     cudaFree(e->d_bits);
@@ -108,6 +110,48 @@ int product(kc_engine *e, double2 *x, const double2 *y) {
     return check_launch(e) ? 0 : e->err;
 }
 
+// A graph of kSquareChunk squarings of x (its kernels take x as an argument); the column
+// inverse tracks round-off on the steps that are multiples of the descriptor's err_every.
+cudaGraphExec_t square_graph(kc_engine *e, double2 *x) {
+    kc_engine::SquareGraph *slot = nullptr;
+    for (auto &g : e->graphs)
+        if (g.exec && g.x == (const double *)x) slot = &g;
+    if (!slot) {
+        slot = &e->graphs[0];
+        for (auto &g : e->graphs)
+            if (!g.exec || g.last_use < slot->last_use) slot = &g;
+        if (slot->exec) cudaGraphExecDestroy(slot->exec);
+        slot->exec = nullptr;
+        slot->x = (const double *)x;
+        cudaGraph_t graph;
+        if (!ok(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal))) return nullptr;
+        for (uint64_t j = 0; j < kSquareChunk; j++) {
+            launch_rows(e->ls, false, x, nullptr, (int)j);
+            launch_col_inverse(e->ls, true, x, (int)j);
+            launch_col_forward(e->ls, x, true, (int)j);
+        }
+        if (!ok(e, cudaStreamEndCapture(e->stream, &graph))) return nullptr;
+        const bool inst = ok(e, cudaGraphInstantiate(&slot->exec, graph, 0));
+        cudaGraphDestroy(graph);
+        if (!inst) return nullptr;
+    }
+    slot->last_use = ++e->graph_clock;
+    return slot->exec;
+}
+
+// count squarings of x: whole chunks from the graph, the rest launched one by one
+int square_many(kc_engine *e, double2 *x, uint64_t count) {
+    while (count >= kSquareChunk) {
+        cudaGraphExec_t g = square_graph(e, x);
+        if (!g || !ok(e, cudaGraphLaunch(g, e->stream))) return e->err ? e->err : -1;
+        count -= kSquareChunk;
+        e->op_count += kSquareChunk;
+    }
+    for (uint64_t i = 0; i < count; i++)
+        if (product(e, x, nullptr)) return e->err;
+    return 0;
+}
+
 int set_addend(kc_engine *e, int64_t c) {
     if (e->add_cached == (c != 0) && e->add_c == c) return 0;
     uint32_t idx[kMaxAddend];
@@ -134,6 +178,14 @@ extern "C" {
 kc_engine *kc_engine_new(uint64_t k, uint64_t n, uint32_t L, const uint8_t *bits, const double *w,
                          const double *oscale, uint32_t top_t, uint64_t top_st, uint32_t top_m,
                          uint64_t sL, int device) {
+    return kc_engine_create(k, n, L, bits, w, oscale, top_t, top_st, top_m, sL, device, false);
+}
+
+}  // extern "C"
+
+kc_engine *kc_engine_create(uint64_t k, uint64_t n, uint32_t L, const uint8_t *bits, const double *w,
+                            const double *oscale, uint32_t top_t, uint64_t top_st, uint32_t top_m,
+                            uint64_t sL, int device, bool throughput) {
     kc_engine *e = new (std::nothrow) kc_engine();
     if (!e) return nullptr;
     if (device < 0 && cudaGetDevice(&device) != cudaSuccess) {
@@ -154,17 +206,35 @@ kc_engine *kc_engine_new(uint64_t k, uint64_t n, uint32_t L, const uint8_t *bits
     }
     const double *wv = w ? w : e->lay.w.data();
     const double *ov = oscale ? oscale : e->lay.oscale.data();
-    e->plan = get_plan(L);
-    if (!e->plan || e->lay.L - e->lay.top_t > 2 * (uint32_t)kGroup) {
+    // a test run alone spreads each pass over the SMs (shape and column-group width chosen for
+    // latency); a batch slot takes the throughput shape and the widest groups
+    const unsigned top_digits = e->lay.L - e->lay.top_t;
+    if (throughput) {
+        e->G = kGroup;
+        e->plan = get_plan(L);
+    } else {
+        unsigned min_bits = 64;
+        for (uint8_t b : e->lay.bits) min_bits = b < min_bits ? b : min_bits;
+        int nsm = 1;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+        uint32_t R = 0, C = 0;
+        int G = kGroup;
+        if (choose_latency_shape(L / 2, nsm, min_bits, top_digits, R, C, G)) {
+            e->G = G;
+            e->plan = get_plan(L, R);
+        }
+    }
+    if (!e->plan || top_digits > 2 * (uint32_t)e->G) {
         delete e;
         return nullptr;
     }
     const LengthPlan &P = *e->plan;
     const uint32_t H = P.H;
+    e->NG = P.C / e->G;
     bool good = ok(e, cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking)) &&
-                dalloc(e, &e->d_desc, 1) && dalloc(e, &e->d_work, P.pairs.size() + P.NG) &&
+                dalloc(e, &e->d_desc, 1) && dalloc(e, &e->d_work, P.pairs.size() + e->NG) &&
                 dalloc(e, &e->d_bits, L) && dalloc(e, &e->d_w, L) && dalloc(e, &e->d_osc, L) &&
-                dalloc(e, &e->d_idig, L) && dalloc(e, &e->d_dig, L) && dalloc(e, &e->d_slot, (size_t)P.NG * P.R) &&
+                dalloc(e, &e->d_idig, L) && dalloc(e, &e->d_dig, L) && dalloc(e, &e->d_slot, (size_t)e->NG * P.R) &&
                 dalloc(e, &e->d_maxerr, 1) && dalloc(e, &e->d_status, 1) &&
                 ok(e, cudaMallocHost((void **)&e->h_dig, (size_t)L * sizeof(long long))) &&
                 ok(e, cudaMallocHost((void **)&e->h_err, sizeof(unsigned long long)));
@@ -177,7 +247,7 @@ kc_engine *kc_engine_new(uint64_t k, uint64_t n, uint32_t L, const uint8_t *bits
         }
         std::vector<WorkItem> work;
         for (size_t i = 0; i < P.pairs.size(); i++) work.push_back({0, (int)i});
-        for (uint32_t g = 0; g < P.NG; g++) work.push_back({0, (int)g});
+        for (uint32_t g = 0; g < e->NG; g++) work.push_back({0, (int)g});
         good = ok(e, cudaMemcpy(e->d_bits, e->lay.bits.data(), L, cudaMemcpyHostToDevice)) &&
                ok(e, cudaMemcpy(e->d_w, wv, L * sizeof(double), cudaMemcpyHostToDevice)) &&
                ok(e, cudaMemcpy(e->d_osc, osc.data(), L * sizeof(double), cudaMemcpyHostToDevice)) &&
@@ -185,7 +255,7 @@ kc_engine *kc_engine_new(uint64_t k, uint64_t n, uint32_t L, const uint8_t *bits
                ok(e, cudaMemcpy(e->d_work, work.data(), work.size() * sizeof(WorkItem), cudaMemcpyHostToDevice)) &&
                ok(e, cudaMemset(e->d_maxerr, 0, sizeof(unsigned long long))) &&
                ok(e, cudaMemset(e->d_status, 0, sizeof(int))) &&
-               ok(e, cudaMemset(e->d_slot, 0, (size_t)P.NG * P.R * sizeof(long long)));
+               ok(e, cudaMemset(e->d_slot, 0, (size_t)e->NG * P.R * sizeof(long long)));
     }
     if (good) {
         TestDesc &d = e->desc;
@@ -193,7 +263,8 @@ kc_engine *kc_engine_new(uint64_t k, uint64_t n, uint32_t L, const uint8_t *bits
         d.H = (int)H;
         d.R = (int)P.R;
         d.C = (int)P.C;
-        d.NG = (int)P.NG;
+        d.NG = (int)e->NG;
+        d.G = e->G;
         d.rp = P.rp;
         d.cp = P.cp;
         d.twr = P.twr;
@@ -228,11 +299,12 @@ kc_engine *kc_engine_new(uint64_t k, uint64_t n, uint32_t L, const uint8_t *bits
         s.rows = e->d_work;
         s.nrows = (int)P.pairs.size();
         s.cols = e->d_work + P.pairs.size();
-        s.ncols = (int)P.NG;
+        s.ncols = (int)e->NG;
         s.grid_rows = s.nrows;
         s.grid_cols = s.ncols;
         s.row_smem_per_lane = (size_t)P.C * sizeof(double2);
-        s.col_smem = (size_t)P.R * kGroup * sizeof(double2);
+        s.col_smem = (size_t)P.R * e->G * sizeof(double2);
+        s.G = e->G;
         good = good && kernels_prepare(s.row_smem_per_lane * 6, s.col_smem) == 0;
     }
     if (!good) {
@@ -242,6 +314,8 @@ kc_engine *kc_engine_new(uint64_t k, uint64_t n, uint32_t L, const uint8_t *bits
     }
     return e;
 }
+
+extern "C" {
 
 void kc_engine_free(kc_engine *e) {
     if (!e) return;
@@ -297,17 +371,13 @@ int kc_to_digits(kc_engine *e, const double *x, int64_t *digits) {
 int kc_square(kc_engine *e, double *x, uint64_t count) {
     DeviceGuard dg(e->device);
     if (e->add_c && set_addend(e, 0)) return e->err ? e->err : -1;
-    for (uint64_t i = 0; i < count; i++)
-        if (product(e, (double2 *)x, nullptr)) return e->err;
-    return 0;
+    return square_many(e, (double2 *)x, count);
 }
 
 int kc_square_add(kc_engine *e, double *x, uint64_t count, int64_t c) {
     DeviceGuard dg(e->device);
     if (set_addend(e, c)) return e->err ? e->err : -1;
-    for (uint64_t i = 0; i < count; i++)
-        if (product(e, (double2 *)x, nullptr)) return e->err;
-    return 0;
+    return square_many(e, (double2 *)x, count);
 }
 
 int kc_mul(kc_engine *e, double *x, const double *y) {
@@ -352,7 +422,14 @@ void kc_reset_maxerr(kc_engine *e) {
     ok(e, cudaMemsetAsync(e->d_maxerr, 0, sizeof(unsigned long long), e->stream));
 }
 
-void kc_set_roundoff_check(kc_engine *e, uint32_t every) { e->err_every = every ? every : 1; }
+void kc_set_roundoff_check(kc_engine *e, uint32_t every) {
+    e->err_every = every ? every : 1;
+    if (e->desc.err_every != (int)e->err_every) {
+        DeviceGuard dg(e->device);
+        e->desc.err_every = (int)e->err_every;  // read by the graphed squarings
+        upload_desc(e);
+    }
+}
 
 int kc_error(const kc_engine *e) { return e->err; }
 
@@ -368,5 +445,7 @@ void kc_shape(const kc_engine *e, uint32_t *R, uint32_t *C) {
     if (R) *R = e->plan->R;
     if (C) *C = e->plan->C;
 }
+
+int kc_group_width(const kc_engine *e) { return e->G; }
 
 }  // extern "C"

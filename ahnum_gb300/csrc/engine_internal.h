@@ -32,7 +32,25 @@ struct kc_engine {
     uint64_t op_count = 0;
     int add_cached = 0;              // constant currently folded in desc (0: none)
     int64_t add_c = 0;
+    int G = 8;                       // columns per column group
+    uint32_t NG = 0;                 // column groups, C / G
+    // squarings of one number replayed from a CUDA graph (kSquareChunk of them per replay),
+    // one graph per recently squared number
+    struct SquareGraph {
+        const double *x = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        uint64_t last_use = 0;
+    } graphs[4];
+    uint64_t graph_clock = 0;
 };
+
+constexpr uint64_t kSquareChunk = 16;
+
+// kc_engine_new for a test run alone (throughput = false: shape and group width chosen for the
+// latency of one squaring) or for a batch slot (throughput = true: the throughput shape, G = 8).
+kc_engine *kc_engine_create(uint64_t k, uint64_t n, uint32_t L, const uint8_t *bits, const double *w,
+                            const double *oscale, uint32_t top_t, uint64_t top_st, uint32_t top_m,
+                            uint64_t sL, int device, bool throughput);
 
 
 // helpers shared with the batch engine (engine.cu)

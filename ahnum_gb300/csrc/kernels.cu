@@ -180,8 +180,8 @@ constexpr double kMagic = 6755399441055744.0;
 constexpr long long kMagicBits = 0x4338000000000000ll;
 
 // load the group's columns times conj(w_H^{c k_r}) into digit-reversed rows of the buffer
+template <int G>
 __device__ __forceinline__ void load_columns_conj(const TestDesc &T, const double2 *x, int g, double2 *sm) {
-    constexpr int G = kGroup;
     const int C = T.C;
     for (int i = threadIdx.x; i < T.R * G; i += blockDim.x) {
         const int kr = i / G, l = i % G;
@@ -190,13 +190,12 @@ __device__ __forceinline__ void load_columns_conj(const TestDesc &T, const doubl
     }
 }
 
-template <bool ERR>
+template <bool ERR, int G>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_inverse(const TestDesc *__restrict__ tests,
                                                           const WorkItem *__restrict__ work,
                                                           int nwork, const int *nwork_dev,
                                                           int step, const double2 *xo) {
     extern __shared__ double2 sm[];
-    constexpr int G = kGroup;
     long long *smd = reinterpret_cast<long long *>(sm);
     if (nwork_dev) nwork = *nwork_dev;
     for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
@@ -206,7 +205,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_inverse(const Test
         const bool track = ERR && (step % T.err_every == 0);
         const double2 *x = xo ? xo : T.x;
         const int R = T.R, C = T.C, g = it.unit;
-        load_columns_conj(T, x, g, sm);
+        load_columns_conj<G>(T, x, g, sm);
         __syncthreads();
         smem_fft<true>(sm, T.cp, T.twc, G, G);
         // unweight, scale and round every value in parallel: one FMA with the magic constant
@@ -260,12 +259,12 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_inverse(const Test
     }
 }
 
+template <int G>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_forward(const TestDesc *__restrict__ tests,
                                                           const WorkItem *__restrict__ work,
                                                           int nwork, const int *nwork_dev, int step,
                                                           double2 *xo, int use_slots) {
     extern __shared__ double2 sm[];
-    constexpr int G = kGroup;
     if (nwork_dev) nwork = *nwork_dev;
     for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
         const WorkItem it = work[wi];
@@ -309,17 +308,17 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_forward(const Test
     }
 }
 
+template <int G>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_digits(const TestDesc *__restrict__ tests,
                                                          const WorkItem *__restrict__ work,
                                                          int nwork, const double2 *xo) {
     extern __shared__ double2 sm[];
-    constexpr int G = kGroup;
     for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
         const WorkItem it = work[wi];
         const TestDesc &T = tests[it.test];
         const double2 *x = xo ? xo : T.x;
         const int R = T.R, C = T.C, g = it.unit;
-        load_columns_conj(T, x, g, sm);
+        load_columns_conj<G>(T, x, g, sm);
         __syncthreads();
         smem_fft<true>(sm, T.cp, T.twc, G, G);
         for (int i = threadIdx.x; i < R * G; i += blockDim.x) {
@@ -369,10 +368,18 @@ int kernels_prepare(size_t row_smem, size_t col_smem) {
         if (!rc) row_hw[dev] = row_smem;
     }
     if (col_smem > col_hw[dev]) {
-        rc |= set_smem((const void *)k_col_inverse<false>, col_smem);
-        rc |= set_smem((const void *)k_col_inverse<true>, col_smem);
-        rc |= set_smem((const void *)k_col_forward, col_smem);
-        rc |= set_smem((const void *)k_col_digits, col_smem);
+        rc |= set_smem((const void *)k_col_inverse<false, 2>, col_smem);
+        rc |= set_smem((const void *)k_col_inverse<true, 2>, col_smem);
+        rc |= set_smem((const void *)k_col_inverse<false, 4>, col_smem);
+        rc |= set_smem((const void *)k_col_inverse<true, 4>, col_smem);
+        rc |= set_smem((const void *)k_col_inverse<false, 8>, col_smem);
+        rc |= set_smem((const void *)k_col_inverse<true, 8>, col_smem);
+        rc |= set_smem((const void *)k_col_forward<2>, col_smem);
+        rc |= set_smem((const void *)k_col_forward<4>, col_smem);
+        rc |= set_smem((const void *)k_col_forward<8>, col_smem);
+        rc |= set_smem((const void *)k_col_digits<2>, col_smem);
+        rc |= set_smem((const void *)k_col_digits<4>, col_smem);
+        rc |= set_smem((const void *)k_col_digits<8>, col_smem);
         if (!rc) col_hw[dev] = col_smem;
     }
     return rc;
@@ -386,20 +393,37 @@ void launch_rows(const LaunchSet &s, bool mul, double2 *x, const double2 *y, int
         k_rows<false><<<s.grid_rows, kThreads, smem, s.stream>>>(s.tests, s.rows, s.nrows, s.nrows_dev, step, x, y);
 }
 
-void launch_col_inverse(const LaunchSet &s, bool err, const double2 *x, int step) {
+template <int G>
+static void col_inverse_g(const LaunchSet &s, bool err, const double2 *x, int step) {
     if (err)
-        k_col_inverse<true><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x);
+        k_col_inverse<true, G><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x);
     else
-        k_col_inverse<false><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x);
+        k_col_inverse<false, G><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x);
+}
+
+void launch_col_inverse(const LaunchSet &s, bool err, const double2 *x, int step) {
+    switch (s.G) {
+    case 2: col_inverse_g<2>(s, err, x, step); break;
+    case 4: col_inverse_g<4>(s, err, x, step); break;
+    default: col_inverse_g<8>(s, err, x, step); break;
+    }
 }
 
 void launch_col_forward(const LaunchSet &s, double2 *x, bool use_slots, int step) {
-    k_col_forward<<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x,
-                                                                   use_slots ? 1 : 0);
+    const int u = use_slots ? 1 : 0;
+    switch (s.G) {
+    case 2: k_col_forward<2><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x, u); break;
+    case 4: k_col_forward<4><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x, u); break;
+    default: k_col_forward<8><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x, u); break;
+    }
 }
 
 void launch_col_digits(const LaunchSet &s, const double2 *x) {
-    k_col_digits<<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, x);
+    switch (s.G) {
+    case 2: k_col_digits<2><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, x); break;
+    case 4: k_col_digits<4><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, x); break;
+    default: k_col_digits<8><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, x); break;
+    }
 }
 
 void launch_elementwise(cudaStream_t st, double2 *x, const double2 *y, size_t n, int op) {

@@ -24,7 +24,8 @@ struct LaunchSet {
     const int *ncols_dev = nullptr;    //   (graphs captured once, lists refilled per launch)
     int grid_rows = 0, grid_cols = 0;
     size_t row_smem_per_lane = 0;      // C * sizeof(double2) for the longest row
-    size_t col_smem = 0;               // R * kGroup * sizeof(double2) for the longest column
+    size_t col_smem = 0;               // R * G * sizeof(double2) for the longest column
+    int G = kGroup;                    // column-group width of every test in the launch
 };
 
 // Raise (never lower) the kernels' dynamic shared-memory limits on the current device; 0 on

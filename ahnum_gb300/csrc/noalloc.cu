@@ -28,13 +28,13 @@ namespace {
 
 constexpr size_t kDescBytes = (sizeof(TestDesc) + 255) / 256 * 256;
 constexpr size_t kDigBytes = (size_t)KC_NOALLOC_MAX_WORDS * sizeof(long long);
-// one carry per (column group, row): H / kGroup of them
-constexpr size_t kSlotBytes = (size_t)KC_NOALLOC_MAX_WORDS / 2 / kGroup * sizeof(long long);
+// one carry per (column group, row): at most H / 2 of them (groups of 2 columns)
+constexpr size_t kSlotBytes = (size_t)KC_NOALLOC_MAX_WORDS / 2 / 2 * sizeof(long long);
 constexpr size_t kScratchBytes = kDescBytes + kDigBytes + kSlotBytes;
 
 }  // namespace
 
-// The scratch itself: ~0.55 MB per device, shared by every call.
+// The scratch itself: ~0.65 MB per device, shared by every call.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 namespace {
@@ -67,7 +67,7 @@ unsigned char *scratch_address(int device, int *err) {
 extern "C" int kc_square_noalloc(kc_engine *e, const double *x, double *y) {
     if (!e || !x || !y) return -1;
     const LengthPlan &P = *e->plan;
-    if (e->lay.L > KC_NOALLOC_MAX_WORDS || (size_t)P.NG * P.R * sizeof(long long) > kSlotBytes)
+    if (e->lay.L > KC_NOALLOC_MAX_WORDS || (size_t)e->NG * P.R * sizeof(long long) > kSlotBytes)
         return KC_NOALLOC_TOO_LARGE;
     int prev = -1;
     cudaGetDevice(&prev);

@@ -101,6 +101,44 @@ bool choose_shape(uint32_t H, uint32_t &R, uint32_t &C) {
     return R != 0;
 }
 
+static int radix_stages(uint32_t n) {
+    int st = 0;
+    for (; n % 4 == 0; n /= 4) st++;
+    for (uint32_t p : {2u, 3u, 5u, 7u})
+        for (; n % p == 0; n /= p) st++;
+    return st;
+}
+
+bool choose_latency_shape(uint32_t H, int nsm, unsigned min_bits, unsigned top_digits, uint32_t &R,
+                          uint32_t &C, int &G) {
+    // FP64 lane-operations per point of each pass (measured: rows ~53, each column pass ~24),
+    // a fixed cost per stage barrier, and the load of the busiest SM.
+    double best = 1e300;
+    R = C = 0;
+    G = kGroup;
+    if (nsm < 1) nsm = 1;
+    for (uint32_t c = 16; c <= 2048 && c <= H / 2; c += kGroup) {
+        if (H % c || !shape_usable(H, H / c, c)) continue;
+        const uint32_t r = H / c;
+        for (int g : {2, 4, 8}) {
+            // the carry into a segment must be absorbed by 2g-1 digits of at least min_bits (a
+            // product's carry stays below 2^(51 - b)), and the top region must fit one segment
+            if ((2 * g - 1) * (int)min_bits < 51 - (int)min_bits || (int)top_digits > 2 * g) continue;
+            const double pairs = r / 2 + 1, groups = c / g;
+            const double rows = std::ceil(pairs / nsm) * 106.0 * c + 800.0 * (2 * radix_stages(c) + 2);
+            const double cols = std::ceil(groups / nsm) * 24.0 * r * g + 800.0 * (radix_stages(r) + 2);
+            const double cost = rows + 2 * cols;
+            if (cost < best - 1e-9) {
+                best = cost;
+                R = r;
+                C = c;
+                G = g;
+            }
+        }
+    }
+    return R != 0;
+}
+
 bool make_fft_plan(int n, FftPlan &pl) {
     // radix 4 throughout the power-of-two part (tangent twiddles), one radix 2 if needed, and
     // the odd radices last: the last plan stage has span 1 and runs without twiddles, so the
@@ -206,15 +244,20 @@ static void stage_twiddles(const FftPlan &pl, std::vector<double2> &tw) {
     }
 }
 
-std::shared_ptr<LengthPlan> build_plan_host(uint32_t L, std::vector<double2> *twr,
+std::shared_ptr<LengthPlan> build_plan_host(uint32_t L, uint32_t rows, std::vector<double2> *twr,
                                             std::vector<double2> *twc, std::vector<double2> *t4,
                                             std::vector<double2> *sw) {
     if (L % (2 * kGroup) || L < 64) return nullptr;
     auto pl = std::make_shared<LengthPlan>();
     pl->L = L;
     pl->H = L / 2;
-    if (!choose_shape(pl->H, pl->R, pl->C)) return nullptr;
-    pl->NG = pl->C / kGroup;
+    if (rows) {
+        if (pl->H % rows || !shape_usable(pl->H, rows, pl->H / rows)) return nullptr;
+        pl->R = rows;
+        pl->C = pl->H / rows;
+    } else if (!choose_shape(pl->H, pl->R, pl->C)) {
+        return nullptr;
+    }
     if (!make_fft_plan((int)pl->C, pl->rp) || !make_fft_plan((int)pl->R, pl->cp)) return nullptr;
     positions(pl->rp, pl->rev_c, pl->pos_c);
     positions(pl->cp, pl->rev_r, pl->pos_r);
@@ -247,18 +290,18 @@ static bool upload(const std::vector<T> &h, T **d, size_t &bytes) {
     return !nb || cudaMemcpy(*d, h.data(), nb, cudaMemcpyHostToDevice) == cudaSuccess;
 }
 
-std::shared_ptr<LengthPlan> get_plan(uint32_t L) {
+std::shared_ptr<LengthPlan> get_plan(uint32_t L, uint32_t R) {
     static std::mutex mu;
     static std::map<std::tuple<int, uint32_t, uint32_t>, std::shared_ptr<LengthPlan>> cache;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
-    uint32_t R = 0, C = 0;
-    if (L % 2 || !choose_shape(L / 2, R, C)) return nullptr;
+    uint32_t C = 0;
+    if (L % 2 || (!R && !choose_shape(L / 2, R, C))) return nullptr;
     std::lock_guard<std::mutex> lock(mu);
     auto it = cache.find({dev, L, R});
     if (it != cache.end()) return it->second;
     std::vector<double2> twr, twc, t4, sw;
-    auto pl = build_plan_host(L, &twr, &twc, &t4, &sw);
+    auto pl = build_plan_host(L, R, &twr, &twc, &t4, &sw);
     if (!pl) return nullptr;
     pl->device = dev;
     bool ok = upload(twr, &pl->twr, pl->device_bytes) && upload(twc, &pl->twc, pl->device_bytes) &&

@@ -11,7 +11,7 @@
 namespace kg {
 
 struct LengthPlan {
-    uint32_t L = 0, H = 0, R = 0, C = 0, NG = 0;
+    uint32_t L = 0, H = 0, R = 0, C = 0;
     FftPlan rp, cp;                   // row plan (C points), column plan (R points)
     std::vector<int> rev_r, pos_r;    // DIF output position <-> frequency, column transform
     std::vector<int> rev_c, pos_c;    // same for the row transform
@@ -38,11 +38,17 @@ bool make_fft_plan(int n, FftPlan &pl);
 // exp(-2 pi i j / m) with the angle reduced exactly in integer arithmetic
 double2 cis_neg(uint64_t j, uint64_t m);
 
-// Cached plan for (current device, L); nullptr if L cannot be planned or the device upload
-// fails.  Thread-safe.
-std::shared_ptr<LengthPlan> get_plan(uint32_t L);
+// Shape and column-group width for one test run alone: spread every pass over the SMs so the
+// squaring's latency, not its total FP64 work, is smallest.  Throughput (batched) use takes
+// choose_shape and G = kGroup instead.  min_bits: the narrowest digit; top_digits: L - top_t.
+bool choose_latency_shape(uint32_t H, int nsm, unsigned min_bits, unsigned top_digits, uint32_t &R,
+                          uint32_t &C, int &G);
+
+// Cached plan for (current device, L, R) (R = 0: choose_shape); nullptr if L cannot be planned or
+// the device upload fails.  Thread-safe.
+std::shared_ptr<LengthPlan> get_plan(uint32_t L, uint32_t R = 0);
 // Host tables only (no device upload).
-std::shared_ptr<LengthPlan> build_plan_host(uint32_t L, std::vector<double2> *twr,
+std::shared_ptr<LengthPlan> build_plan_host(uint32_t L, uint32_t R, std::vector<double2> *twr,
                                             std::vector<double2> *twc, std::vector<double2> *t4,
                                             std::vector<double2> *sw);
 

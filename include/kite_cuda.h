@@ -71,6 +71,9 @@ int kc_sync(kc_engine *e);
 void *kc_stream(kc_engine *e);
 /* Four-step shape chosen for the engine's length: H = R * C complex points. */
 void kc_shape(const kc_engine *e, uint32_t *R, uint32_t *C);
+/* Columns per column-pass work unit (2, 4 or 8): an engine created by kc_engine_new spreads each
+ * pass of one squaring over the SMs; batch slots use 8. */
+int kc_group_width(const kc_engine *e);
 
 /* ---- a squaring that allocates nothing ---------------------------------------------------
  * No counterpart in the reference (its backends run on the host and never allocate device
@@ -79,7 +82,7 @@ void kc_shape(const kc_engine *e, uint32_t *R, uint32_t *C);
  * cannot allocate when they need the product: code running during a CUDA stream capture, a
  * plugin whose host owns the device memory through its own pool, or a latency-bound loop that
  * cannot afford the device synchronisation of an allocation.  Its scratch is one static device
- * array of about 0.55 MB that every GPU loading this library reserves until the process exits.
+ * array of about 0.65 MB that every GPU loading this library reserves until the process exits.
  *   - lengths above KC_NOALLOC_MAX_WORDS words are refused with KC_NOALLOC_TOO_LARGE;
  *   - the first call on a device looks up the array's device address (cudaGetSymbolAddress)
  *     with that device current: make that first call before any stream capture begins;
