@@ -52,6 +52,7 @@ class Verdict:
     squarings: int
     runs: int = 1
     rc: int = 0
+    factor: int = 0         # LLR: the small factor that decided the test, else 0
 
     @property
     def latency(self) -> float:
@@ -179,7 +180,8 @@ class Server:
                     continue
                 # LLR: a factor or V == 0 decides at once; a non-zero V is confirmed
                 if res.factor:
-                    verdicts.append(Verdict(r.rid, r.kind, r.k, r.n, 0, False, r.arrival, done_t, 0, 0.0, 0))
+                    verdicts.append(Verdict(r.rid, r.kind, r.k, r.n, 0, False, r.arrival, done_t, 0, 0.0, 0,
+                                            factor=int(res.factor)))
                     continue
                 run.res64s.append(res.res64)
                 run.zeros.append(bool(res.is_prp))
@@ -254,7 +256,7 @@ def main():
     for v in sorted(verdicts, key=lambda v: v.rid):
         print(json.dumps({"id": v.rid, "kind": v.kind, "k": v.k, "n": v.n, "res64": f"{v.res64:016X}",
                           "prime": v.is_prime, "latency_s": round(v.latency, 3), "fft_len": v.fft_len,
-                          "maxerr": round(v.maxerr, 4), "runs": v.runs, "rc": v.rc}))
+                          "maxerr": round(v.maxerr, 4), "runs": v.runs, "rc": v.rc, "factor": v.factor}))
 
 
 if __name__ == "__main__":

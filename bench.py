@@ -55,6 +55,20 @@ def workload(seed: int = SEED, count: int = SLOTS):
     return [(int(k), int(n)) for k, n in zip(ks, ns)]
 
 
+def combine_ranks(t_block: float, t_block_wall: float, per_rank_units: float, dist=None):
+    """Replicas: every rank ran its own batch.  The step time is the slowest rank's (max over
+    ranks) and the whole-job throughput is the sum of the ranks' units over that time, i.e.
+    world x units / max time.  Returns (t_block, t_block_wall, world)."""
+    world = 1
+    if dist is not None and dist.is_initialized():
+        import torch
+        world = dist.get_world_size()
+        tt = torch.tensor([t_block, t_block_wall], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_block, t_block_wall = float(tt[0]), float(tt[1])
+    return t_block, t_block_wall, world
+
+
 def rank_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -225,13 +239,8 @@ def run_ours(args):
             gpu_ms.append(ms.value)
     if dist:
         dist.barrier()
-    t_block = statistics.mean(gpu_ms) * 1e-3
-    t_block_wall = statistics.mean(wall)
-    if dist:
-        import torch
-        tt = torch.tensor([t_block, t_block_wall], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_block, t_block_wall = float(tt[0]), float(tt[1])
+    t_block, t_block_wall, _ = combine_ranks(statistics.mean(gpu_ms) * 1e-3, statistics.mean(wall),
+                                             SLOTS, dist)
 
     ovh = 1 + 1 / BLOCKS_PER_CHECK
     per_rank = 3600.0 * SLOTS * BLOCK / (t_block * ovh * mean_n)
