@@ -1,5 +1,5 @@
-"""ctypes binding of libkite_gb300.so: the kite C API (include/kite.h) and the engine C ABI
-(include/kite_cuda.h).
+"""ctypes binding of libkite_gb300.so: the kite C API (include/kite.h), the engine C ABI
+(include/kite_cuda.h) and the PRST-compatible proof API (include/kite_proof.h).
 
 The library is the product; this module only declares its prototypes.  Loading fails loudly
 when the library has not been built: there is no Python or CPU fallback.
@@ -48,6 +48,11 @@ class KitePrpResult(C.Structure):
                 ("resumed_at", C.c_uint64), ("seconds", C.c_double)]
 
 
+class PpGiant(C.Structure):
+    """pp_giant (include/kite_proof.h): little-endian 32-bit words, no leading zeros."""
+    _fields_ = [("w", u32p), ("len", C.c_int32)]
+
+
 class KiteLlrOpts(C.Structure):
     _fields_ = [("fft", KiteOpts), ("max_roundoff", C.c_double), ("checkpoint", C.c_char_p),
                 ("checkpoint_secs", C.c_double), ("progress", PROGRESS_FN),
@@ -74,6 +79,8 @@ class KcTestResult(C.Structure):
 
 
 KITE_BACKEND_CUDA = 5
+PP_TYPE_VALUE, PP_TYPE_PRODUCT, PP_TYPE_CERT = 1, 3, 4
+PP_ABORTED = -2
 KC_TEST_FERMAT = 0
 KC_TEST_LLR = 1
 
@@ -164,6 +171,23 @@ PROTOTYPES = {
     "kc_limbs_to_digits": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, u64p, i64p]),
     "kc_carry_digits": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, i64p]),
     "kc_choose_fft_len": (C.c_uint32, [C.c_uint64, C.c_uint64]),
+    # PRST-compatible proofs (include/kite_proof.h)
+    "pp_giant_free": (None, [C.POINTER(PpGiant)]),
+    "pp_fingerprint": (C.c_uint32, [C.c_uint64, C.c_uint64]),
+    "pp_unique_fingerprint": (C.c_uint32, [C.c_uint32, C.c_char_p]),
+    "pp_proof_fingerprint": (C.c_uint32, [C.c_uint64, C.c_uint64, C.c_uint32]),
+    "pp_write": (C.c_int, [C.c_char_p, C.c_int, C.c_uint32, C.c_int32, C.POINTER(PpGiant), C.c_int]),
+    "pp_read": (C.c_int, [C.c_char_p, C.c_int, C.c_uint32, C.POINTER(C.c_int32), C.POINTER(PpGiant),
+                          C.c_int]),
+    "pp_points": (C.c_int, [C.c_uint32, C.c_int, u32p]),
+    "pp_from_num": (None, [vp, vp, C.POINTER(PpGiant)]),
+    "pp_to_num": (None, [vp, vp, C.POINTER(PpGiant)]),
+    "pp_res64": (C.c_uint64, [C.POINTER(PpGiant)]),
+    "pp_save_products": (C.c_int, [vp, C.c_uint64, C.c_uint64, C.c_uint32, C.c_int, C.c_char_p, C.c_int,
+                                   C.POINTER(C.c_int), u64p]),
+    "pp_build_cert": (C.c_int, [vp, C.c_uint64, C.c_uint64, C.c_uint32, C.c_int, C.c_char_p, C.c_int,
+                                u64p]),
+    "pp_verify_cert": (C.c_int, [vp, C.c_uint64, C.c_uint64, C.c_char_p, u64p, u32p]),
 }
 
 _lock = threading.Lock()
