@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -86,6 +87,7 @@ struct kc_batch {
     size_t graph_row_smem = 0, graph_col_smem = 0;
     uint32_t graph_B = 0;
     int grid = 0;
+    int threads = 128;  // block size of the pass kernels
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int err = 0;
     const char *what = "";      // the step that failed, for kc_batch_error_string
@@ -145,6 +147,7 @@ LaunchSet launch_set(kc_batch *b, const kc_batch::Lists &l, size_t row_lane, siz
     s.ncols_dev = l.d_cnt + 1;
     s.grid_rows = b->grid;
     s.grid_cols = b->grid;
+    s.threads = b->threads;
     s.row_smem_per_lane = row_lane;
     s.col_smem = col_smem;
     return s;
@@ -467,7 +470,13 @@ kc_batch *kc_batch_new(int device, uint32_t gerbicz_block, uint32_t gerbicz_bloc
     cudaMemGetInfo(&fr, &tot);
     b->budget = mem_budget ? mem_budget : fr / 10 * 8;
     cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, device);
-    b->grid = b->nsm * kMinBlocks;
+    // Block size of the pass kernels: 128 threads, so that 8 CTAs share an SM with the register
+    // budget (64 per thread) of 4 CTAs of 256.  Measured on GB300 over the 256-test workload:
+    // 1.034 s per 1000-squaring block at 128 threads, 1.103 s at 256 and 1.103 s at 64.
+    // KITE_GB300_BATCH_THREADS=256 selects the larger blocks.
+    b->threads = 128;
+    if (const char *t = getenv("KITE_GB300_BATCH_THREADS")) b->threads = atoi(t) == 256 ? 256 : 128;
+    b->grid = b->nsm * (kThreads * kMinBlocks / b->threads);
     if (!bok(b, cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) || !bok(b, cudaEventCreate(&b->ev0)) ||
         !bok(b, cudaEventCreate(&b->ev1))) {
         kc_batch_free(b);

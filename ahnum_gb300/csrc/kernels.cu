@@ -388,17 +388,17 @@ int kernels_prepare(size_t row_smem, size_t col_smem) {
 void launch_rows(const LaunchSet &s, bool mul, double2 *x, const double2 *y, int step) {
     const size_t smem = s.row_smem_per_lane * (mul ? 6 : 4);
     if (mul)
-        k_rows<true><<<s.grid_rows, kThreads, smem, s.stream>>>(s.tests, s.rows, s.nrows, s.nrows_dev, step, x, y);
+        k_rows<true><<<s.grid_rows, s.threads, smem, s.stream>>>(s.tests, s.rows, s.nrows, s.nrows_dev, step, x, y);
     else
-        k_rows<false><<<s.grid_rows, kThreads, smem, s.stream>>>(s.tests, s.rows, s.nrows, s.nrows_dev, step, x, y);
+        k_rows<false><<<s.grid_rows, s.threads, smem, s.stream>>>(s.tests, s.rows, s.nrows, s.nrows_dev, step, x, y);
 }
 
 template <int G>
 static void col_inverse_g(const LaunchSet &s, bool err, const double2 *x, int step) {
     if (err)
-        k_col_inverse<true, G><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x);
+        k_col_inverse<true, G><<<s.grid_cols, s.threads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x);
     else
-        k_col_inverse<false, G><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x);
+        k_col_inverse<false, G><<<s.grid_cols, s.threads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x);
 }
 
 void launch_col_inverse(const LaunchSet &s, bool err, const double2 *x, int step) {
@@ -412,17 +412,17 @@ void launch_col_inverse(const LaunchSet &s, bool err, const double2 *x, int step
 void launch_col_forward(const LaunchSet &s, double2 *x, bool use_slots, int step) {
     const int u = use_slots ? 1 : 0;
     switch (s.G) {
-    case 2: k_col_forward<2><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x, u); break;
-    case 4: k_col_forward<4><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x, u); break;
-    default: k_col_forward<8><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x, u); break;
+    case 2: k_col_forward<2><<<s.grid_cols, s.threads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x, u); break;
+    case 4: k_col_forward<4><<<s.grid_cols, s.threads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x, u); break;
+    default: k_col_forward<8><<<s.grid_cols, s.threads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x, u); break;
     }
 }
 
 void launch_col_digits(const LaunchSet &s, const double2 *x) {
     switch (s.G) {
-    case 2: k_col_digits<2><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, x); break;
-    case 4: k_col_digits<4><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, x); break;
-    default: k_col_digits<8><<<s.grid_cols, kThreads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, x); break;
+    case 2: k_col_digits<2><<<s.grid_cols, s.threads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, x); break;
+    case 4: k_col_digits<4><<<s.grid_cols, s.threads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, x); break;
+    default: k_col_digits<8><<<s.grid_cols, s.threads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, x); break;
     }
 }
 

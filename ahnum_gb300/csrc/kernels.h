@@ -26,6 +26,7 @@ struct LaunchSet {
     size_t row_smem_per_lane = 0;      // C * sizeof(double2) for the longest row
     size_t col_smem = 0;               // R * G * sizeof(double2) for the longest column
     int G = kGroup;                    // column-group width of every test in the launch
+    int threads = kThreads;            // block size: 256, or 128 for twice the CTAs per SM
 };
 
 // Raise (never lower) the kernels' dynamic shared-memory limits on the current device; 0 on
