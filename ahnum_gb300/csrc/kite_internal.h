@@ -6,14 +6,19 @@
 
 #include "../../include/kite.h"
 #include "../../include/kite_cuda.h"
+#include "../../include/kite_ntt.h"
 #include "layout.h"
 
 struct kite_ctx {
     kg::Layout lay;            // exact digit layout, weights, N
-    kc_engine *eng = nullptr;  // device engine for this modulus
+    kc_engine *eng = nullptr;  // FP64 IBDWT engine for this modulus, or
+    kn_engine *ntt = nullptr;  // the integer-NTT engine (KITE_BACKEND_CUDA_NTT)
     std::vector<int64_t> dig;  // L digits of host scratch
 };
 
 struct kite_num {
-    double *d = nullptr;  // device memory, kc_num_doubles() doubles
+    void *d = nullptr;  // device memory: kc_num_doubles() doubles, or kn_num_words() words
 };
+
+// x <- x^2 + c, count times, on the context's engine (the LLR doubling with c = -2)
+int kite_square_add_internal(kite_ctx *ctx, kite_num *x, uint64_t count, int64_t c);

@@ -9,7 +9,8 @@
 // decides if they disagree.
 //
 // The doubling V <- V^2 - 2 runs entirely on the device: the -2 is added to the rounded digits
-// inside the normaliser (kc_square_add), so a step is one squaring with no extra pass.
+// inside the normaliser (kc_square_add; the NTT engine adds it in its reduction), so a step is
+// one squaring with no extra pass.
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -163,13 +164,13 @@ int llr_run(uint64_t k, uint64_t n, uint32_t P, const kite_llr_opts &o, uint32_t
             const uint64_t stop = i + B < total ? i + B : total;
             while (i < stop) {
                 if (i == 0) {  // V_{2k} = V_k^2 + 2
-                    kc_square_add(ctx->eng, x->d, 1, 2);
+                    kite_square_add_internal(ctx, x, 1, 2);
                     i++;
                     continue;
                 }
                 uint64_t upto = stop;
                 if (fault_due && o.inject_fault_at > i && o.inject_fault_at < upto) upto = o.inject_fault_at;
-                kc_square_add(ctx->eng, x->d, upto - i, -2);
+                kite_square_add_internal(ctx, x, upto - i, -2);
                 i = upto;
                 if (fault_due && i == o.inject_fault_at) {
                     kite_debug_corrupt(ctx, x);

@@ -1,0 +1,931 @@
+// Exact integer-NTT squaring modulo N = k*2^n - 1 (include/kite_ntt.h).
+//
+// One modular squaring is four kernels over a test's W words of w bits:
+//   kn_col_fwd   per group of G columns of the R x C four-step layout: words -> residues modulo
+//                four primes, forward column NTT (decimation in frequency, natural order in,
+//                bit-reversed out), times the four-step twiddle w_NP^(k_r c).
+//   kn_rows      per row: forward row NTT (DIF), pointwise Montgomery square or product,
+//                inverse row NTT (decimation in time, bit-reversed in, natural out).
+//   kn_col_inv   per column group: times w_NP^(-k_r c) 2^32 / NP, inverse column NTT (DIT),
+//                Garner CRT of the four residues into the exact coefficient (< 2^120).
+//   kn_reduce    per test, one block: carry the coefficients into words of P = x^2, Montgomery
+//                reduction P 2^-n == B + k A (mod N) for P = A + B 2^n, A < 2^n, plus an
+//                optional constant, carry, and the top fold T 2^n == q + r 2^n for T = q k + r.
+// Reference: gpu/ntt_reg.metal:90-246 (the four-step NTT passes), gpu/sq.metal:23-192 (residues,
+// Garner CRT, carry, REDC, fold), gpu/gpu_ctx.h:57-322 (tables and the pass sequence).
+//
+// Modular arithmetic (p < 2^30, so 4p < 2^32): residues stay in [0, 2p) between operations
+// (Harvey's lazy butterflies); a twiddle w is applied as Shoup's x*w - floor(x*w'/2^32)*p with
+// w' = floor(w*2^32/p); pointwise products use Montgomery's reduction by 2^32, whose 2^-32 the
+// inverse twiddles undo.  Every kernel is integer-only: IMAD, IADD3, IMNMX, LOP3 on the
+// integer pipes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "../../include/kite_ntt.h"
+
+namespace kn {
+
+using u128 = unsigned __int128;
+
+constexpr int kPrimes = 4;
+// p = m 2^e + 1 below 2^30 with 15 | m and e >= 20: transforms of length 2^a, 3 2^a, 5 2^a for
+// a <= 20 exist modulo every one; their product is 2^119.36.
+constexpr uint32_t kP[kPrimes] = {1053818881u, 975175681u, 943718401u, 880803841u};
+constexpr int kG = 8;                // columns per column group
+constexpr int kColThreads = 256;
+constexpr int kRowThreads = 256;
+constexpr int kReduceThreads = 512;
+
+struct Prime {
+    uint32_t p;
+    uint32_t pinv;  // -p^-1 mod 2^32
+    uint2 one;      // Shoup pair of 1: reduces any 32-bit value to [0, 2p)
+    uint2 r32;      // Shoup pair of 2^32 mod p
+};
+
+struct Tables {
+    const uint2 *twr_f[kPrimes], *twr_i[kPrimes];  // length-R level tables, [s + j] = w_2s^(+-j)
+    const uint2 *twc_f[kPrimes], *twc_i[kPrimes];  // length-C level tables
+    const uint2 *t4_f[kPrimes], *t4_i[kPrimes];    // [pos_r * C + c], storage order
+};
+
+// Garner constants: Shoup pairs of p_i^-1 mod p_j
+struct Crt {
+    uint2 inv01, inv02, inv12, inv03, inv13, inv23;
+};
+
+struct Desc {
+    uint32_t NP, R, C, NU;      // NU: coefficients that can be non-zero (2W - 1, rounded up)
+    uint32_t W, w, WN0, BN0;    // words, word bits, n / w, n % w
+    uint64_t k;
+    uint64_t *x;                // operand and result
+    const uint64_t *y;          // second operand of a product
+    uint32_t *res, *res2;       // 4 NP residues each
+    ulonglong2 *coef;           // NP exact coefficients (lo, hi)
+    uint64_t *pw;               // NP words of the product
+    const uint64_t *addend;     // W words added after the reduction, or null
+    int *status;                // non-zero: a carry left the number (cannot happen for valid input)
+    Prime pr[kPrimes];
+    Crt crt;
+    Tables tb;
+};
+
+// ---- device arithmetic ------------------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t red2(uint32_t v, uint32_t m) { return min(v, v - m); }  // [0,2m) -> [0,m)
+
+__device__ __forceinline__ uint32_t shoup(uint32_t x, uint2 w, uint32_t p) {
+    const uint32_t q = __umulhi(x, w.y);
+    return x * w.x - q * p;  // in [0, 2p) for any 32-bit x
+}
+
+__device__ __forceinline__ uint32_t montmul(uint32_t a, uint32_t b, uint32_t p, uint32_t pinv) {
+    const uint64_t t = (uint64_t)a * b;  // a, b < 2p: t < 4p^2 < 2^62
+    const uint32_t m = (uint32_t)t * pinv;
+    return (uint32_t)((t + (uint64_t)m * p) >> 32);  // a b 2^-32 mod p, in [0, 2p)
+}
+
+__device__ __forceinline__ uint32_t residue(uint64_t word, const Prime &P) {
+    const uint32_t lo = (uint32_t)word, hi = (uint32_t)(word >> 32);
+    return red2(shoup(lo, P.one, P.p) + shoup(hi, P.r32, P.p), 2 * P.p);
+}
+
+// Forward DIF stage of half-size s over `nt` interleaved transforms of length n stored at
+// buf[t_off(t) + e * st]: (a, b) -> (a + b, (a - b) w_2s^j).
+__device__ __forceinline__ void dif_stage(uint32_t *buf, int n, int s, int nl, int stride_l, int st,
+                                          const Desc &D, const uint2 *const *tw, int nprime_groups,
+                                          int group_stride) {
+    const int half = n / 2;
+    const int total = nprime_groups * nl * half;
+    for (int q = threadIdx.x; q < total; q += blockDim.x) {
+        const int l = q % nl;
+        const int t = q / nl;
+        const int b = t % half, i = t / half;
+        const int j = b % s, i0 = (b / s) * 2 * s + j;
+        uint32_t *base = buf + i * group_stride + l * stride_l;
+        const uint32_t p = D.pr[i].p, p2 = 2 * p;
+        const uint32_t a = base[i0 * st], c = base[(i0 + s) * st];
+        base[i0 * st] = red2(a + c, p2);
+        base[(i0 + s) * st] = shoup(a - c + p2, __ldg(&tw[i][s + j]), p);
+    }
+}
+
+// Inverse DIT stage of half-size s: (a, b) -> (a + b w, a - b w), w = w_2s^-j.
+__device__ __forceinline__ void dit_stage(uint32_t *buf, int n, int s, int nl, int stride_l, int st,
+                                          const Desc &D, const uint2 *const *tw, int nprime_groups,
+                                          int group_stride) {
+    const int half = n / 2;
+    const int total = nprime_groups * nl * half;
+    for (int q = threadIdx.x; q < total; q += blockDim.x) {
+        const int l = q % nl;
+        const int t = q / nl;
+        const int b = t % half, i = t / half;
+        const int j = b % s, i0 = (b / s) * 2 * s + j;
+        uint32_t *base = buf + i * group_stride + l * stride_l;
+        const uint32_t p = D.pr[i].p, p2 = 2 * p;
+        const uint32_t a = base[i0 * st];
+        const uint32_t c = shoup(base[(i0 + s) * st], __ldg(&tw[i][s + j]), p);
+        base[i0 * st] = red2(a + c, p2);
+        base[(i0 + s) * st] = red2(a - c + p2, p2);
+    }
+}
+
+// ---- pass kernels -----------------------------------------------------------------------------
+
+// shared memory [prime][r][l], l < kG
+// src overrides the test's operand (x, or y for the second operand of a product)
+__global__ void __launch_bounds__(kColThreads) kn_col_fwd(const Desc *descs, const int2 *items, int nitems,
+                                                          int second, const uint64_t *src_o) {
+    extern __shared__ uint32_t sm[];
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const int2 wi = items[it];
+        const Desc &D = descs[wi.x];
+        const int R = (int)D.R, C = (int)D.C, g = wi.y;
+        const uint64_t *src = src_o ? src_o : (second ? D.y : D.x);
+        uint32_t *dst = second ? D.res2 : D.res;
+        for (int e = threadIdx.x; e < R * kG; e += blockDim.x) {
+            const int r = e / kG, l = e % kG;
+            const uint32_t j = (uint32_t)r * C + g * kG + l;
+            const uint64_t word = j < D.W ? src[j] : 0;
+#pragma unroll
+            for (int i = 0; i < kPrimes; i++) sm[(i * R + r) * kG + l] = residue(word, D.pr[i]);
+        }
+        __syncthreads();
+        for (int s = R / 2; s >= 1; s >>= 1) {
+            dif_stage(sm, R, s, kG, 1, kG, D, D.tb.twr_f, kPrimes, R * kG);
+            __syncthreads();
+        }
+        for (int e = threadIdx.x; e < kPrimes * R * kG; e += blockDim.x) {
+            const int l = e % kG, t = e / kG, pos = t % R, i = t / R;
+            const uint32_t m = (uint32_t)pos * C + g * kG + l;
+            dst[(size_t)i * D.NP + m] = shoup(sm[(i * R + pos) * kG + l], __ldg(&D.tb.t4_f[i][m]), D.pr[i].p);
+        }
+        __syncthreads();
+    }
+}
+
+// shared memory [operand][prime][c]
+template <bool MUL>
+__global__ void __launch_bounds__(kRowThreads) kn_rows(const Desc *descs, const int2 *items, int nitems) {
+    extern __shared__ uint32_t sm[];
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const int2 wi = items[it];
+        const Desc &D = descs[wi.x];
+        const int C = (int)D.C, pos = wi.y;
+        for (int e = threadIdx.x; e < kPrimes * C; e += blockDim.x) {
+            const int i = e / C, c = e % C;
+            const size_t m = (size_t)i * D.NP + (size_t)pos * C + c;
+            sm[i * C + c] = D.res[m];
+            if (MUL) sm[(kPrimes + i) * C + c] = D.res2[m];
+        }
+        __syncthreads();
+        for (int s = C / 2; s >= 1; s >>= 1) {
+            dif_stage(sm, C, s, 1, 0, 1, D, D.tb.twc_f, kPrimes, C);
+            if (MUL) dif_stage(sm + kPrimes * C, C, s, 1, 0, 1, D, D.tb.twc_f, kPrimes, C);
+            __syncthreads();
+        }
+        for (int e = threadIdx.x; e < kPrimes * C; e += blockDim.x) {
+            const int i = e / C;
+            const uint32_t a = sm[e];
+            sm[e] = montmul(a, MUL ? sm[kPrimes * C + e] : a, D.pr[i].p, D.pr[i].pinv);
+        }
+        __syncthreads();
+        for (int s = 1; s < C; s <<= 1) {
+            dit_stage(sm, C, s, 1, 0, 1, D, D.tb.twc_i, kPrimes, C);
+            __syncthreads();
+        }
+        for (int e = threadIdx.x; e < kPrimes * C; e += blockDim.x) {
+            const int i = e / C, c = e % C;
+            D.res[(size_t)i * D.NP + (size_t)pos * C + c] = sm[i * C + c];
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ uint32_t sub_mod(uint32_t a, uint32_t b, uint32_t p) {  // a, b in [0, p)
+    return red2(a + p - b, p);
+}
+
+// exact coefficient from residues v_i in [0, p_i) (Garner's mixed radix)
+__device__ __forceinline__ ulonglong2 garner(const uint32_t *v, const Desc &D) {
+    const uint32_t p0 = D.pr[0].p, p1 = D.pr[1].p, p2 = D.pr[2].p, p3 = D.pr[3].p;
+    const uint32_t x0 = v[0];
+    const uint32_t x1 = red2(shoup(sub_mod(v[1], red2(x0, p1), p1), D.crt.inv01, p1), p1);
+    uint32_t t = red2(shoup(sub_mod(v[2], red2(x0, p2), p2), D.crt.inv02, p2), p2);
+    const uint32_t x2 = red2(shoup(sub_mod(t, red2(x1, p2), p2), D.crt.inv12, p2), p2);
+    t = red2(shoup(sub_mod(v[3], red2(x0, p3), p3), D.crt.inv03, p3), p3);
+    t = red2(shoup(sub_mod(t, red2(x1, p3), p3), D.crt.inv13, p3), p3);
+    const uint32_t x3 = red2(shoup(sub_mod(t, red2(x2, p3), p3), D.crt.inv23, p3), p3);
+    const uint64_t h = x2 + (uint64_t)p2 * x3;                 // < 2^60
+    u128 c = (u128)x1 + (u128)p1 * h;                          // < 2^90
+    c = (u128)x0 + (u128)p0 * c;                               // < 2^120
+    return make_ulonglong2((unsigned long long)c, (unsigned long long)(c >> 64));
+}
+
+__global__ void __launch_bounds__(kColThreads) kn_col_inv(const Desc *descs, const int2 *items, int nitems) {
+    extern __shared__ uint32_t sm[];
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const int2 wi = items[it];
+        const Desc &D = descs[wi.x];
+        const int R = (int)D.R, C = (int)D.C, g = wi.y;
+        for (int e = threadIdx.x; e < kPrimes * R * kG; e += blockDim.x) {
+            const int l = e % kG, t = e / kG, pos = t % R, i = t / R;
+            const uint32_t m = (uint32_t)pos * C + g * kG + l;
+            sm[(i * R + pos) * kG + l] = shoup(D.res[(size_t)i * D.NP + m], __ldg(&D.tb.t4_i[i][m]), D.pr[i].p);
+        }
+        __syncthreads();
+        for (int s = 1; s < R; s <<= 1) {
+            dit_stage(sm, R, s, kG, 1, kG, D, D.tb.twr_i, kPrimes, R * kG);
+            __syncthreads();
+        }
+        for (int e = threadIdx.x; e < R * kG; e += blockDim.x) {
+            const int r = e / kG, l = e % kG;
+            const uint32_t j = (uint32_t)r * C + g * kG + l;
+            uint32_t v[kPrimes];
+#pragma unroll
+            for (int i = 0; i < kPrimes; i++) v[i] = red2(sm[(i * R + r) * kG + l], D.pr[i].p);
+            D.coef[j] = j < D.NU ? garner(v, D) : make_ulonglong2(0, 0);
+        }
+        __syncthreads();
+    }
+}
+
+// Carries pending at chunk boundaries: co[t] is the carry out of chunk t (S words at t S) into
+// chunk t + 1.  Adds them in until none is left; returns (in every thread) the carry that left
+// the top of v.
+__device__ u128 resolve_chunks(uint64_t *v, uint32_t len, uint32_t S, uint32_t w, u128 *co, u128 *top) {
+    const int t = threadIdx.x, T = blockDim.x;
+    const uint64_t M = (w == 64) ? ~0ull : ((1ull << w) - 1);
+    if (t == 0) *top = 0;
+    for (;;) {
+        __syncthreads();
+        const u128 cin = t > 0 ? co[t - 1] : 0;
+        if (t == T - 1) *top += co[T - 1];
+        __syncthreads();
+        u128 acc = cin;
+        uint32_t j = (uint32_t)t * S;
+        const uint32_t e = min(len, j + S);
+        for (; acc != 0 && j < e; j++) {
+            acc += v[j];
+            v[j] = (uint64_t)acc & M;
+            acc >>= w;
+        }
+        co[t] = acc;
+        if (!__syncthreads_or(acc != 0)) break;
+    }
+    __syncthreads();
+    return *top;
+}
+
+// x_o, add_o override the test's result array and addend
+__global__ void __launch_bounds__(kReduceThreads) kn_reduce(const Desc *descs, const int *tests, uint64_t *x_o,
+                                                            const uint64_t *add_o) {
+    __shared__ u128 co[kReduceThreads];
+    __shared__ u128 top;
+    const Desc &D = descs[tests[blockIdx.x]];
+    uint64_t *X = x_o ? x_o : D.x;
+    const uint64_t *addend = x_o ? add_o : D.addend;
+    const int t = threadIdx.x, T = blockDim.x;
+    const uint32_t w = D.w;
+    const uint64_t M = (1ull << w) - 1;
+    // 1. product words: P = sum coef_j 2^(w j)
+    {
+        const uint32_t S = (D.NU + T - 1) / T;
+        u128 acc = 0;
+        const uint32_t j0 = (uint32_t)t * S, e = min(D.NU, j0 + S);
+        for (uint32_t j = j0; j < e; j++) {
+            const ulonglong2 c = D.coef[j];
+            acc += ((u128)c.y << 64) | c.x;
+            D.pw[j] = (uint64_t)acc & M;
+            acc >>= w;
+        }
+        co[t] = acc;
+        if (resolve_chunks(D.pw, D.NU, S, w, co, &top) != 0 && t == 0) atomicOr(D.status, 1);
+    }
+    // 2. Montgomery reduction E = B + k A (+ addend), P = A + B 2^n
+    {
+        const uint32_t S = (D.W + T - 1) / T;
+        const uint32_t WN0 = D.WN0, BN0 = D.BN0, NU = D.NU;
+        const uint64_t lowmask = (1ull << BN0) - 1;
+        u128 acc = 0;
+        const uint32_t j0 = (uint32_t)t * S, e = min(D.W, j0 + S);
+        for (uint32_t j = j0; j < e; j++) {
+            const uint64_t a = j < WN0 ? D.pw[j] : (j == WN0 ? (D.pw[j] & lowmask) : 0);
+            const uint32_t s = WN0 + j;
+            const uint64_t lo = s < NU ? D.pw[s] : 0, hi = s + 1 < NU ? D.pw[s + 1] : 0;
+            const uint64_t b = BN0 ? (((lo >> BN0) | (hi << (w - BN0))) & M) : lo;
+            acc += (u128)b + (u128)D.k * a + (addend ? addend[j] : 0);
+            X[j] = (uint64_t)acc & M;
+            acc >>= w;
+        }
+        co[t] = acc;
+        if (resolve_chunks(X, D.W, S, w, co, &top) != 0 && t == 0) atomicOr(D.status, 2);
+    }
+    // 3. top fold: T = x >> n = q k + r; x <- x mod 2^n + q + r 2^n
+    if (t == 0) {
+        uint64_t *x = X;
+        const uint32_t WN0 = D.WN0, BN0 = D.BN0;
+        u128 Tv = x[WN0] >> BN0;
+        uint32_t sh = w - BN0;
+        for (uint32_t j = WN0 + 1; j < D.W; j++) {
+            if (x[j]) {
+                if (sh >= 128 || (sh > 64 && (x[j] >> (128 - sh)) != 0)) atomicOr(D.status, 4);
+                else Tv |= (u128)x[j] << sh;
+            }
+            sh += w;
+            x[j] = 0;
+        }
+        x[WN0] &= (1ull << BN0) - 1;
+        const u128 q = Tv / D.k;
+        const uint64_t r = (uint64_t)(Tv - q * D.k);
+        u128 add = (u128)r << BN0;
+        for (uint32_t j = WN0; add != 0 && j < D.W; j++) {
+            add += x[j];
+            x[j] = (uint64_t)add & M;
+            add >>= w;
+        }
+        if (add) atomicOr(D.status, 8);
+        add = q;
+        for (uint32_t j = 0; add != 0 && j < D.W; j++) {
+            add += x[j];
+            x[j] = (uint64_t)add & M;
+            add >>= w;
+        }
+        if (add) atomicOr(D.status, 8);
+    }
+}
+
+// ---- host tables ------------------------------------------------------------------------------
+
+uint32_t mulmod(uint32_t a, uint32_t b, uint32_t p) { return (uint32_t)((uint64_t)a * b % p); }
+uint32_t powmod(uint32_t a, uint64_t e, uint32_t p) {
+    uint32_t r = 1 % p;
+    for (; e; e >>= 1, a = mulmod(a, a, p))
+        if (e & 1) r = mulmod(r, a, p);
+    return r;
+}
+uint32_t invmod(uint32_t a, uint32_t p) { return powmod(a % p, p - 2, p); }
+uint2 shoup_pair(uint32_t w, uint32_t p) { return make_uint2(w, (uint32_t)(((uint64_t)w << 32) / p)); }
+
+// a generator of the multiplicative group mod p (p - 1 = m 2^e with m's prime factors small)
+uint32_t generator(uint32_t p) {
+    std::vector<uint32_t> f;
+    uint32_t m = p - 1;
+    for (uint32_t q = 2; q * q <= m; q++)
+        if (m % q == 0) {
+            f.push_back(q);
+            while (m % q == 0) m /= q;
+        }
+    if (m > 1) f.push_back(m);
+    for (uint32_t g = 2;; g++) {
+        bool ok = true;
+        for (uint32_t q : f)
+            if (powmod(g, (p - 1) / q, p) == 1) {
+                ok = false;
+                break;
+            }
+        if (ok) return g;
+    }
+}
+
+uint32_t bitrev(uint32_t x, int bits) {
+    uint32_t r = 0;
+    for (int b = 0; b < bits; b++) r |= ((x >> b) & 1u) << (bits - 1 - b);
+    return r;
+}
+
+int ilog2(uint32_t x) {
+    int b = 0;
+    while ((1u << b) < x) b++;
+    return b;
+}
+
+struct Plan {
+    uint32_t NP = 0, R = 0, C = 0;
+    uint2 *d_tables = nullptr;  // one allocation for every table
+    Tables tb{};
+    ~Plan() {
+        if (d_tables) cudaFree(d_tables);
+    }
+};
+
+// level tables of a length-n transform: [s + j] = w_2s^(dir j), s = 1, 2, .., n/2, j < s
+void level_table(std::vector<uint2> &out, uint32_t n, uint32_t wn, uint32_t p) {
+    // wn: a primitive n-th root; w_2s = wn^(n / 2s)
+    out.assign(n, make_uint2(0, 0));
+    for (uint32_t s = 1; s < n; s <<= 1) {
+        const uint32_t w2s = powmod(wn, n / (2 * s), p);
+        uint32_t v = 1;
+        for (uint32_t j = 0; j < s; j++, v = mulmod(v, w2s, p)) out[s + j] = shoup_pair(v, p);
+    }
+}
+
+std::mutex g_plan_mu;
+std::map<std::pair<int, uint32_t>, std::shared_ptr<Plan>> g_plans;
+
+std::shared_ptr<Plan> get_plan(int device, uint32_t NP) {
+    std::lock_guard<std::mutex> lock(g_plan_mu);
+    auto key = std::make_pair(device, NP);
+    auto itp = g_plans.find(key);
+    if (itp != g_plans.end()) return itp->second;
+    auto P = std::make_shared<Plan>();
+    P->NP = NP;
+    const int a = ilog2(NP);
+    P->R = 1u << (a / 2);
+    P->C = NP / P->R;
+    const uint32_t R = P->R, C = P->C;
+    const int logR = ilog2(R);
+    // layout per prime: twr_f[R], twr_i[R], twc_f[C], twc_i[C], t4_f[NP], t4_i[NP]
+    const size_t per = 2 * (size_t)R + 2 * (size_t)C + 2 * (size_t)NP;
+    std::vector<uint2> host(per * kPrimes);
+    std::vector<uint2> tmp;
+    for (int i = 0; i < kPrimes; i++) {
+        const uint32_t p = kP[i];
+        const uint32_t g = generator(p);
+        const uint32_t wN = powmod(g, (p - 1) / NP, p), wNi = invmod(wN, p);
+        uint2 *base = host.data() + per * i;
+        level_table(tmp, R, powmod(wN, C, p), p);
+        std::copy(tmp.begin(), tmp.end(), base);
+        level_table(tmp, R, powmod(wNi, C, p), p);
+        std::copy(tmp.begin(), tmp.end(), base + R);
+        level_table(tmp, C, powmod(wN, R, p), p);
+        std::copy(tmp.begin(), tmp.end(), base + 2 * R);
+        level_table(tmp, C, powmod(wNi, R, p), p);
+        std::copy(tmp.begin(), tmp.end(), base + 2 * R + C);
+        // four-step twiddles in storage order: position pos holds frequency k_r = bitrev(pos)
+        const uint32_t scale = mulmod(invmod(NP % p, p), (uint32_t)((1ull << 32) % p), p);
+        uint2 *t4f = base + 2 * R + 2 * C, *t4i = t4f + NP;
+        for (uint32_t pos = 0; pos < R; pos++) {
+            const uint32_t kr = bitrev(pos, logR);
+            const uint32_t a1 = powmod(wN, kr, p), a1i = powmod(wNi, kr, p);
+            uint32_t v = 1, vi = scale;
+            for (uint32_t c = 0; c < C; c++) {
+                t4f[pos * C + c] = shoup_pair(v, p);
+                t4i[pos * C + c] = shoup_pair(vi, p);
+                v = mulmod(v, a1, p);
+                vi = mulmod(vi, a1i, p);
+            }
+        }
+    }
+    if (cudaMalloc((void **)&P->d_tables, host.size() * sizeof(uint2)) != cudaSuccess) return nullptr;
+    if (cudaMemcpy(P->d_tables, host.data(), host.size() * sizeof(uint2), cudaMemcpyHostToDevice) != cudaSuccess)
+        return nullptr;
+    for (int i = 0; i < kPrimes; i++) {
+        const uint2 *base = P->d_tables + per * i;
+        P->tb.twr_f[i] = base;
+        P->tb.twr_i[i] = base + R;
+        P->tb.twc_f[i] = base + 2 * R;
+        P->tb.twc_i[i] = base + 2 * R + C;
+        P->tb.t4_f[i] = base + 2 * R + 2 * C;
+        P->tb.t4_i[i] = base + 2 * R + 2 * C + NP;
+    }
+    g_plans[key] = P;
+    return P;
+}
+
+// ---- exact host integers (64-bit limbs) -------------------------------------------------------
+
+// N = k 2^n - 1 in nl limbs
+std::vector<uint64_t> modulus(uint64_t k, uint64_t n, size_t nl) {
+    std::vector<uint64_t> N(nl, 0);
+    const u128 kk = (u128)k << (n % 64);
+    N[n / 64] = (uint64_t)kk;
+    if (n / 64 + 1 < nl) N[n / 64 + 1] = (uint64_t)(kk >> 64);
+    for (size_t j = 0; j < nl; j++)
+        if (N[j]--) break;
+    return N;
+}
+
+bool geq(const std::vector<uint64_t> &a, const std::vector<uint64_t> &b) {
+    for (size_t j = a.size(); j-- > 0;)
+        if (a[j] != b[j]) return a[j] > b[j];
+    return true;
+}
+
+void sub_in(std::vector<uint64_t> &a, const std::vector<uint64_t> &b) {
+    uint64_t br = 0;
+    for (size_t j = 0; j < a.size(); j++) {
+        const u128 d = (u128)a[j] - b[j] - br;
+        a[j] = (uint64_t)d;
+        br = (uint64_t)(d >> 64) ? 1 : 0;
+    }
+}
+
+}  // namespace kn
+
+using namespace kn;
+
+struct kn_engine {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t k = 0, n = 0;
+    uint32_t W = 0, w = 0, NP = 0;
+    size_t nlimbs = 0;
+    std::vector<uint64_t> N;         // modulus, nlimbs limbs (+1 spare)
+    std::shared_ptr<Plan> plan;
+    Desc desc{};
+    Desc *d_desc = nullptr;
+    int2 *d_cols = nullptr, *d_rows = nullptr;
+    int *d_test = nullptr;
+    int *d_status = nullptr;
+    uint32_t *d_res = nullptr, *d_res2 = nullptr;
+    ulonglong2 *d_coef = nullptr;
+    uint64_t *d_pw = nullptr;
+    uint64_t *d_addend = nullptr;
+    int64_t addend_c = 0;
+    bool addend_ok = false;
+    int err = 0;
+};
+
+namespace {
+
+bool kok(kn_engine *e, cudaError_t c) {
+    if (c != cudaSuccess && !e->err) e->err = (int)c;
+    return c == cudaSuccess;
+}
+
+// x = sum words[j] 2^(w j) as nl limbs (words may be up to 64 bits wide)
+void words_to_limbs(const uint64_t *words, uint32_t W, uint32_t w, std::vector<uint64_t> &l) {
+    std::fill(l.begin(), l.end(), 0);
+    for (uint32_t j = 0; j < W; j++) {
+        const uint64_t bit = (uint64_t)w * j;
+        const size_t li = bit / 64;
+        const unsigned sh = bit % 64;
+        u128 v = (u128)words[j] << sh;
+        for (size_t t = li; v != 0 && t < l.size(); t++) {
+            v += l[t];
+            l[t] = (uint64_t)v;
+            v >>= 64;
+        }
+    }
+}
+
+void limbs_to_words(const std::vector<uint64_t> &l, uint32_t W, uint32_t w, uint64_t *words) {
+    const uint64_t M = (1ull << w) - 1;
+    for (uint32_t j = 0; j < W; j++) {
+        const uint64_t bit = (uint64_t)w * j;
+        const size_t li = bit / 64;
+        const unsigned sh = bit % 64;
+        u128 v = li < l.size() ? (u128)l[li] : 0;
+        if (li + 1 < l.size()) v |= (u128)l[li + 1] << 64;
+        words[j] = (uint64_t)(v >> sh) & M;
+    }
+}
+
+// v mod N for v of any size (limbs, little endian), using k 2^n == 1: v = T 2^n + L,
+// T = q k + r -> v == L + q + r 2^n
+void reduce_mod(const kn_engine *e, std::vector<uint64_t> v, std::vector<uint64_t> &out) {
+    const uint64_t n = e->n, k = e->k;
+    for (;;) {
+        // T = v >> n
+        const size_t s0 = n / 64;
+        const unsigned sh = n % 64;
+        std::vector<uint64_t> T;
+        for (size_t j = s0; j < v.size(); j++) {
+            u128 cur = v[j] >> sh;
+            if (sh && j + 1 < v.size()) cur |= (u128)v[j + 1] << (64 - sh);
+            T.push_back((uint64_t)cur);
+        }
+        while (!T.empty() && T.back() == 0) T.pop_back();
+        if (T.empty() || (T.size() == 1 && T[0] < k)) break;  // v < k 2^n = N + 1
+        // L = v mod 2^n
+        v.resize(s0 + 1);
+        v[s0] &= sh ? ((1ull << sh) - 1) : 0;
+        if (!sh) v.resize(s0);
+        // q = T / k, r = T mod k
+        u128 rem = 0;
+        for (size_t j = T.size(); j-- > 0;) {
+            const u128 cur = (rem << 64) | T[j];
+            T[j] = (uint64_t)(cur / k);
+            rem = cur % k;
+        }
+        // v += q + r 2^n
+        const size_t need = std::max(v.size(), T.size()) + (n + 64) / 64 + 2;
+        v.resize(need, 0);
+        u128 c = 0;
+        for (size_t j = 0; j < v.size(); j++) {
+            c += (u128)v[j] + (j < T.size() ? T[j] : 0);
+            v[j] = (uint64_t)c;
+            c >>= 64;
+        }
+        u128 add = (u128)(uint64_t)rem << sh;
+        for (size_t j = s0; add != 0 && j < v.size(); j++) {
+            add += v[j];
+            v[j] = (uint64_t)add;
+            add >>= 64;
+        }
+        while (v.size() > e->nlimbs && v.back() == 0) v.pop_back();
+    }
+    v.resize(e->nlimbs + 1, 0);
+    std::vector<uint64_t> N = e->N;
+    N.resize(e->nlimbs + 1, 0);
+    while (geq(v, N)) sub_in(v, N);
+    out.assign(v.begin(), v.begin() + e->nlimbs);
+}
+
+// Montgomery form x~ = x 2^n mod N of x in [0, N): x = q k + r -> x 2^n == q + r 2^n
+void to_mont(const kn_engine *e, const uint64_t *limbs, std::vector<uint64_t> &out) {
+    std::vector<uint64_t> q(limbs, limbs + e->nlimbs);
+    u128 rem = 0;
+    for (size_t j = q.size(); j-- > 0;) {
+        const u128 cur = (rem << 64) | q[j];
+        q[j] = (uint64_t)(cur / e->k);
+        rem = cur % e->k;
+    }
+    q.resize(e->nlimbs + 2, 0);
+    u128 add = (u128)(uint64_t)rem << (e->n % 64);
+    for (size_t j = e->n / 64; add != 0 && j < q.size(); j++) {
+        add += q[j];
+        q[j] = (uint64_t)add;
+        add >>= 64;
+    }
+    out.swap(q);
+}
+
+// A constant c as Montgomery words (a representative in [0, N)).
+bool constant_words(kn_engine *e, int64_t c, std::vector<uint64_t> &words) {
+    std::vector<uint64_t> v(e->nlimbs, 0);
+    if (c >= 0) {
+        v[0] = (uint64_t)c;
+    } else {
+        v = e->N;
+        std::vector<uint64_t> m(e->nlimbs, 0);
+        m[0] = (uint64_t)(-c);
+        sub_in(v, m);
+    }
+    std::vector<uint64_t> mont;
+    to_mont(e, v.data(), mont);
+    std::vector<uint64_t> red;
+    reduce_mod(e, mont, red);  // keep the representative below N
+    words.assign(e->W, 0);
+    limbs_to_words(red, e->W, e->w, words.data());
+    return true;
+}
+
+// transform length and word size for n: the largest w <= 50 whose coefficients stay below the
+// primes' product, among those that give the smallest power-of-2 length >= 2W
+void choose_sizes(uint64_t k, uint64_t n, uint32_t &w, uint32_t &W, uint32_t &NP) {
+    int kb = 0;
+    while (kb < 63 && (k >> kb) > 0) kb++;
+    const uint64_t bits = n + 2 * (uint64_t)kb + 8;
+    uint32_t best_np = 0;
+    for (uint32_t ww = 50; ww >= 24; ww--) {
+        const uint64_t Wc = (bits + ww - 1) / ww;
+        const int lw = ilog2((uint32_t)Wc);
+        if (2 * ww + lw + 1 > 119) continue;
+        uint64_t np = 64;
+        while (np < 2 * Wc) np <<= 1;
+        if (!best_np || np < best_np) {
+            best_np = (uint32_t)np;
+            w = ww;
+            W = (uint32_t)Wc;
+        }
+    }
+    NP = best_np;
+}
+
+}  // namespace
+
+extern "C" {
+
+kn_engine *kn_engine_new(uint64_t k, uint64_t n, int device) {
+    if (!(k & 1) || k >= (1ull << 30) || n < 8 || n > (1ull << 26)) return nullptr;
+    if (device < 0 && cudaGetDevice(&device) != cudaSuccess) return nullptr;
+    if (cudaSetDevice(device) != cudaSuccess) return nullptr;
+    kn_engine *e = new (std::nothrow) kn_engine();
+    if (!e) return nullptr;
+    e->device = device;
+    e->k = k;
+    e->n = n;
+    choose_sizes(k, n, e->w, e->W, e->NP);
+    if (!e->NP || e->NP > (1u << 20)) {
+        delete e;
+        return nullptr;
+    }
+    e->nlimbs = (size_t)((n + 64 + 63) / 64);
+    e->N = modulus(k, n, e->nlimbs);
+    e->plan = get_plan(device, e->NP);
+    if (!e->plan) {
+        delete e;
+        return nullptr;
+    }
+    const uint32_t R = e->plan->R, C = e->plan->C, NP = e->NP;
+    bool ok = kok(e, cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking)) &&
+              kok(e, cudaMalloc((void **)&e->d_desc, sizeof(Desc))) &&
+              kok(e, cudaMalloc((void **)&e->d_res, (size_t)kPrimes * NP * 4)) &&
+              kok(e, cudaMalloc((void **)&e->d_res2, (size_t)kPrimes * NP * 4)) &&
+              kok(e, cudaMalloc((void **)&e->d_coef, (size_t)NP * sizeof(ulonglong2))) &&
+              kok(e, cudaMalloc((void **)&e->d_pw, (size_t)NP * 8)) &&
+              kok(e, cudaMalloc((void **)&e->d_addend, (size_t)e->W * 8)) &&
+              kok(e, cudaMalloc((void **)&e->d_status, sizeof(int))) &&
+              kok(e, cudaMalloc((void **)&e->d_cols, (C / kG) * sizeof(int2))) &&
+              kok(e, cudaMalloc((void **)&e->d_rows, R * sizeof(int2))) &&
+              kok(e, cudaMalloc((void **)&e->d_test, sizeof(int)));
+    if (ok) {
+        std::vector<int2> cols(C / kG), rows(R);
+        for (uint32_t g = 0; g < C / kG; g++) cols[g] = make_int2(0, (int)g);
+        for (uint32_t r = 0; r < R; r++) rows[r] = make_int2(0, (int)r);
+        const int zero = 0;
+        ok = kok(e, cudaMemcpy(e->d_cols, cols.data(), cols.size() * sizeof(int2), cudaMemcpyHostToDevice)) &&
+             kok(e, cudaMemcpy(e->d_rows, rows.data(), rows.size() * sizeof(int2), cudaMemcpyHostToDevice)) &&
+             kok(e, cudaMemcpy(e->d_test, &zero, sizeof zero, cudaMemcpyHostToDevice)) &&
+             kok(e, cudaMemcpy(e->d_status, &zero, sizeof zero, cudaMemcpyHostToDevice));
+    }
+    if (ok) {
+        const size_t col_smem = (size_t)kPrimes * R * kG * 4, row_smem = (size_t)2 * kPrimes * C * 4;
+        ok = kok(e, cudaFuncSetAttribute(kn_col_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)col_smem)) &&
+             kok(e, cudaFuncSetAttribute(kn_col_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)col_smem)) &&
+             kok(e, cudaFuncSetAttribute(kn_rows<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)row_smem)) &&
+             kok(e, cudaFuncSetAttribute(kn_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)row_smem));
+    }
+    if (!ok) {
+        kn_engine_free(e);
+        return nullptr;
+    }
+    Desc &d = e->desc;
+    d.NP = NP;
+    d.R = R;
+    d.C = C;
+    d.W = e->W;
+    d.NU = std::min<uint32_t>(NP, 2 * e->W);
+    d.w = e->w;
+    d.WN0 = (uint32_t)(n / e->w);
+    d.BN0 = (uint32_t)(n % e->w);
+    d.k = k;
+    d.res = e->d_res;
+    d.res2 = e->d_res2;
+    d.coef = e->d_coef;
+    d.pw = e->d_pw;
+    d.status = e->d_status;
+    d.tb = e->plan->tb;
+    for (int i = 0; i < kPrimes; i++) {
+        const uint32_t p = kP[i];
+        uint32_t inv = 1;
+        for (int t = 0; t < 5; t++) inv *= 2 - p * inv;  // p^-1 mod 2^32 by Newton steps
+        d.pr[i].p = p;
+        d.pr[i].pinv = (uint32_t)(0u - inv);
+        d.pr[i].one = shoup_pair(1, p);
+        d.pr[i].r32 = shoup_pair((uint32_t)((1ull << 32) % p), p);
+    }
+    d.crt.inv01 = shoup_pair(invmod(kP[0] % kP[1], kP[1]), kP[1]);
+    d.crt.inv02 = shoup_pair(invmod(kP[0] % kP[2], kP[2]), kP[2]);
+    d.crt.inv12 = shoup_pair(invmod(kP[1] % kP[2], kP[2]), kP[2]);
+    d.crt.inv03 = shoup_pair(invmod(kP[0] % kP[3], kP[3]), kP[3]);
+    d.crt.inv13 = shoup_pair(invmod(kP[1] % kP[3], kP[3]), kP[3]);
+    d.crt.inv23 = shoup_pair(invmod(kP[2] % kP[3], kP[3]), kP[3]);
+    // operands are kernel arguments: the descriptor is written once
+    if (!kok(e, cudaMemcpy(e->d_desc, &d, sizeof d, cudaMemcpyHostToDevice))) {
+        kn_engine_free(e);
+        return nullptr;
+    }
+    return e;
+}
+
+void kn_engine_free(kn_engine *e) {
+    if (!e) return;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    for (void *p : {(void *)e->d_desc, (void *)e->d_res, (void *)e->d_res2, (void *)e->d_coef, (void *)e->d_pw,
+                    (void *)e->d_addend, (void *)e->d_status, (void *)e->d_cols, (void *)e->d_rows, (void *)e->d_test})
+        if (p) cudaFree(p);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+}
+
+uint32_t kn_num_words(const kn_engine *e) { return e ? e->W : 0; }
+uint32_t kn_word_bits(const kn_engine *e) { return e ? e->w : 0; }
+uint32_t kn_transform_len(const kn_engine *e) { return e ? e->NP : 0; }
+size_t kn_limbs(const kn_engine *e) { return e ? e->nlimbs : 0; }
+
+uint64_t *kn_num_alloc(kn_engine *e) {
+    if (!e || e->err) return nullptr;
+    cudaSetDevice(e->device);
+    uint64_t *x = nullptr;
+    if (!kok(e, cudaMalloc((void **)&x, (size_t)e->W * 8))) return nullptr;
+    if (!kok(e, cudaMemsetAsync(x, 0, (size_t)e->W * 8, e->stream))) {
+        cudaFree(x);
+        return nullptr;
+    }
+    return x;
+}
+
+void kn_num_free(kn_engine *e, uint64_t *x) {
+    if (!e || !x) return;
+    cudaSetDevice(e->device);
+    cudaStreamSynchronize(e->stream);
+    cudaFree(x);
+}
+
+int kn_set_limbs(kn_engine *e, uint64_t *x, const uint64_t *limbs) {
+    if (!e || e->err) return -1;
+    std::vector<uint64_t> mont;
+    to_mont(e, limbs, mont);
+    std::vector<uint64_t> words(e->W);
+    limbs_to_words(mont, e->W, e->w, words.data());
+    cudaSetDevice(e->device);
+    if (!kok(e, cudaMemcpyAsync(x, words.data(), (size_t)e->W * 8, cudaMemcpyHostToDevice, e->stream))) return -1;
+    return kok(e, cudaStreamSynchronize(e->stream)) ? 0 : -1;
+}
+
+int kn_get_limbs(kn_engine *e, const uint64_t *x, uint64_t *limbs) {
+    if (!e || e->err) return -1;
+    std::vector<uint64_t> words(e->W);
+    cudaSetDevice(e->device);
+    if (!kok(e, cudaMemcpyAsync(words.data(), x, (size_t)e->W * 8, cudaMemcpyDeviceToHost, e->stream)) ||
+        !kok(e, cudaStreamSynchronize(e->stream)))
+        return -1;
+    int st = 0;
+    if (!kok(e, cudaMemcpy(&st, e->d_status, sizeof st, cudaMemcpyDeviceToHost))) return -1;
+    if (st) {
+        e->err = -100 - st;
+        return -1;
+    }
+    // x = x~ 2^-n = x~ k (mod N)
+    std::vector<uint64_t> v((size_t)e->W * e->w / 64 + 3, 0);
+    words_to_limbs(words.data(), e->W, e->w, v);
+    u128 c = 0;
+    for (auto &l : v) {
+        c += (u128)l * e->k;
+        l = (uint64_t)c;
+        c >>= 64;
+    }
+    v.push_back((uint64_t)c);
+    std::vector<uint64_t> out;
+    reduce_mod(e, v, out);
+    std::copy(out.begin(), out.end(), limbs);
+    return 0;
+}
+
+static int run_product(kn_engine *e, uint64_t *x, const uint64_t *y, const uint64_t *addend) {
+    const uint32_t R = e->plan->R, C = e->plan->C;
+    const size_t col_smem = (size_t)kPrimes * R * kG * 4, row_smem = (size_t)kPrimes * C * 4;
+    const int ncols = (int)(C / kG), nrows = (int)R;
+    kn_col_fwd<<<ncols, kColThreads, col_smem, e->stream>>>(e->d_desc, e->d_cols, ncols, 0, x);
+    if (y) {
+        kn_col_fwd<<<ncols, kColThreads, col_smem, e->stream>>>(e->d_desc, e->d_cols, ncols, 1, y);
+        kn_rows<true><<<nrows, kRowThreads, 2 * row_smem, e->stream>>>(e->d_desc, e->d_rows, nrows);
+    } else {
+        kn_rows<false><<<nrows, kRowThreads, row_smem, e->stream>>>(e->d_desc, e->d_rows, nrows);
+    }
+    kn_col_inv<<<ncols, kColThreads, col_smem, e->stream>>>(e->d_desc, e->d_cols, ncols);
+    kn_reduce<<<1, kReduceThreads, 0, e->stream>>>(e->d_desc, e->d_test, x, addend);
+    return kok(e, cudaGetLastError()) ? 0 : -1;
+}
+
+int kn_square(kn_engine *e, uint64_t *x, uint64_t count) {
+    if (!e || e->err) return -1;
+    cudaSetDevice(e->device);
+    for (uint64_t i = 0; i < count; i++)
+        if (run_product(e, x, nullptr, nullptr)) return -1;
+    return 0;
+}
+
+int kn_square_add(kn_engine *e, uint64_t *x, uint64_t count, int64_t c) {
+    if (!e || e->err) return -1;
+    cudaSetDevice(e->device);
+    if (!e->addend_ok || e->addend_c != c) {
+        std::vector<uint64_t> words;
+        constant_words(e, c, words);
+        if (!kok(e, cudaMemcpyAsync(e->d_addend, words.data(), (size_t)e->W * 8, cudaMemcpyHostToDevice, e->stream)) ||
+            !kok(e, cudaStreamSynchronize(e->stream)))
+            return -1;
+        e->addend_c = c;
+        e->addend_ok = true;
+    }
+    for (uint64_t i = 0; i < count; i++)
+        if (run_product(e, x, nullptr, e->d_addend)) return -1;
+    return 0;
+}
+
+int kn_mul(kn_engine *e, uint64_t *x, const uint64_t *y) {
+    if (!e || e->err) return -1;
+    cudaSetDevice(e->device);
+    return run_product(e, x, y, nullptr);
+}
+
+int kn_copy(kn_engine *e, uint64_t *dst, const uint64_t *src) {
+    if (!e || e->err) return -1;
+    cudaSetDevice(e->device);
+    if (dst == src) return 0;
+    return kok(e, cudaMemcpyAsync(dst, src, (size_t)e->W * 8, cudaMemcpyDeviceToDevice, e->stream)) ? 0 : -1;
+}
+
+int kn_error(const kn_engine *e) { return e ? e->err : -1; }
+
+int kn_sync(kn_engine *e) {
+    if (!e) return -1;
+    cudaSetDevice(e->device);
+    kok(e, cudaStreamSynchronize(e->stream));
+    return e->err;
+}
+
+}  // extern "C"

@@ -13,6 +13,7 @@ from dataclasses import dataclass
 from . import native
 
 CUDA = native.KITE_BACKEND_CUDA
+CUDA_NTT = native.KITE_BACKEND_CUDA_NTT
 
 
 def _limbs_from_int(v: int, nl: int):
@@ -151,11 +152,11 @@ class PrpResult:
 def prp(k: int, n: int, base: int = 3, fft_len: int = 0, gerbicz_block: int = 0,
         gerbicz_blocks: int = 0, inject_fault_at: int = 0, checkpoint: str | None = None,
         checkpoint_unverified: str | None = None, checkpoint_secs: float = 0.0,
-        unverified_secs: float = 0.0, max_roundoff: float = 0.0) -> PrpResult:
-    """kite_prp on the CUDA backend."""
+        unverified_secs: float = 0.0, max_roundoff: float = 0.0, backend: int = CUDA) -> PrpResult:
+    """kite_prp on a CUDA backend (the FP64 engine, or CUDA_NTT)."""
     lib = native.load()
     o = native.KitePrpOpts()
-    o.fft = native.KiteOpts(CUDA, fft_len, 0, 0)
+    o.fft = native.KiteOpts(backend, fft_len, 0, 0)
     o.gerbicz_block = gerbicz_block
     o.gerbicz_blocks = gerbicz_blocks
     o.max_roundoff = max_roundoff
@@ -186,11 +187,11 @@ class LlrResult:
 
 def llr(k: int, n: int, fft_len: int = 0, inject_fault_at: int = 0, inject_fault_runs: int = 0,
         inject_roundoff_at: int = 0, inject_roundoff_ladder: int = 0,
-        checkpoint: str | None = None) -> LlrResult:
-    """kite_llr on the CUDA backend."""
+        checkpoint: str | None = None, backend: int = CUDA) -> LlrResult:
+    """kite_llr on a CUDA backend (the FP64 engine, or CUDA_NTT)."""
     lib = native.load()
     o = native.KiteLlrOpts()
-    o.fft = native.KiteOpts(CUDA, fft_len, 0, 0)
+    o.fft = native.KiteOpts(backend, fft_len, 0, 0)
     o.inject_fault_at = inject_fault_at
     o.inject_fault_runs = inject_fault_runs
     o.inject_roundoff_at = inject_roundoff_at

@@ -1,5 +1,6 @@
 """ctypes binding of libkite_gb300.so: the kite C API (include/kite.h), the engine C ABI
-(include/kite_cuda.h) and the PRST-compatible proof API (include/kite_proof.h).
+(include/kite_cuda.h), the integer-NTT engine (include/kite_ntt.h) and the PRST-compatible proof
+API (include/kite_proof.h).
 
 The library is the product; this module only declares its prototypes.  Loading fails loudly
 when the library has not been built: there is no Python or CPU fallback.
@@ -79,6 +80,7 @@ class KcTestResult(C.Structure):
 
 
 KITE_BACKEND_CUDA = 5
+KITE_BACKEND_CUDA_NTT = 6
 PP_TYPE_VALUE, PP_TYPE_PRODUCT, PP_TYPE_CERT = 1, 3, 4
 PP_ABORTED = -2
 KC_TEST_FERMAT = 0
@@ -171,6 +173,23 @@ PROTOTYPES = {
     "kc_limbs_to_digits": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, u64p, i64p]),
     "kc_carry_digits": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, i64p]),
     "kc_choose_fft_len": (C.c_uint32, [C.c_uint64, C.c_uint64]),
+    # the integer-NTT engine (include/kite_ntt.h)
+    "kn_engine_new": (vp, [C.c_uint64, C.c_uint64, C.c_int]),
+    "kn_engine_free": (None, [vp]),
+    "kn_num_words": (C.c_uint32, [vp]),
+    "kn_word_bits": (C.c_uint32, [vp]),
+    "kn_transform_len": (C.c_uint32, [vp]),
+    "kn_num_alloc": (vp, [vp]),
+    "kn_num_free": (None, [vp, vp]),
+    "kn_limbs": (C.c_size_t, [vp]),
+    "kn_set_limbs": (C.c_int, [vp, vp, u64p]),
+    "kn_get_limbs": (C.c_int, [vp, vp, u64p]),
+    "kn_square": (C.c_int, [vp, vp, C.c_uint64]),
+    "kn_square_add": (C.c_int, [vp, vp, C.c_uint64, C.c_int64]),
+    "kn_mul": (C.c_int, [vp, vp, vp]),
+    "kn_copy": (C.c_int, [vp, vp, vp]),
+    "kn_error": (C.c_int, [vp]),
+    "kn_sync": (C.c_int, [vp]),
     # PRST-compatible proofs (include/kite_proof.h)
     "pp_giant_free": (None, [C.POINTER(PpGiant)]),
     "pp_fingerprint": (C.c_uint32, [C.c_uint64, C.c_uint64]),

@@ -4,7 +4,8 @@
  * This header declares the same types, names, argument meanings and error conventions as the
  * reference library's include/kite.h (kite 0.1.8, include/kite.h:17-169), so code written
  * against that header links against libkite_gb300.so unchanged.  The one addition is
- * KITE_BACKEND_CUDA, the value the reference's `--backend cuda` selects.
+ * KITE_BACKEND_CUDA, the value the reference's `--backend cuda` selects, and KITE_BACKEND_CUDA_NTT,
+ * an exact integer-transform engine for cross-checks.
  *
  * Numbers are opaque: a kite_num lives in GPU memory in the engine's transformed
  * representation.  Every entry point here is host-callable; none needs a CUDA context from the
@@ -36,6 +37,9 @@ typedef enum {
     KITE_BACKEND_SME = 3,
     KITE_BACKEND_C2P = 4,
     KITE_BACKEND_CUDA = 5,
+    /* The exact integer-NTT engine (include/kite_ntt.h): the arithmetic of the reference's GPU
+     * prototype (gpu/sq.metal), no round-off; kite_max_roundoff stays 0. */
+    KITE_BACKEND_CUDA_NTT = 6,
 } kite_backend;
 
 /* Context options (reference include/kite.h:28-35). */

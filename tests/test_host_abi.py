@@ -13,14 +13,14 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def _declared_functions():
     names = []
-    for h in ("kite.h", "kite_cuda.h", "kite_proof.h"):
+    for h in ("kite.h", "kite_cuda.h", "kite_proof.h", "kite_ntt.h"):
         with open(os.path.join(ROOT, "include", h)) as f:
             src = f.read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
         src = re.sub(r"//[^\n]*", "", src)
         for m in re.finditer(r"\b([a-z_][a-z0-9_]*)\s*\(", src):
             name = m.group(1)
-            if name.startswith(("kite_", "kc_", "pp_")) and not name.endswith("_fn"):
+            if name.startswith(("kite_", "kc_", "pp_", "kn_")) and not name.endswith("_fn"):
                 names.append(name)
     # drop function-pointer field names inside structs
     return sorted(set(n for n in names if n not in ("progress", "on_point", "on_confirm")))
