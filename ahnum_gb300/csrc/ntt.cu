@@ -99,45 +99,137 @@ __device__ __forceinline__ uint32_t residue(uint64_t word, const Prime &P) {
     return red2(shoup(lo, P.one, P.p) + shoup(hi, P.r32, P.p), 2 * P.p);
 }
 
-// Forward DIF stage of half-size s over `nt` interleaved transforms of length n stored at
-// buf[t_off(t) + e * st]: (a, b) -> (a + b, (a - b) w_2s^j).
-__device__ __forceinline__ void dif_stage(uint32_t *buf, int n, int s, int nl, int stride_l, int st,
-                                          const Desc &D, const uint2 *const *tw, int nprime_groups,
-                                          int group_stride) {
-    const int half = n / 2;
-    const int total = nprime_groups * nl * half;
-    for (int q = threadIdx.x; q < total; q += blockDim.x) {
-        const int l = q % nl;
-        const int t = q / nl;
-        const int b = t % half, i = t / half;
-        const int j = b % s, i0 = (b / s) * 2 * s + j;
-        uint32_t *base = buf + i * group_stride + l * stride_l;
-        const uint32_t p = D.pr[i].p, p2 = 2 * p;
-        const uint32_t a = base[i0 * st], c = base[(i0 + s) * st];
-        base[i0 * st] = red2(a + c, p2);
-        base[(i0 + s) * st] = shoup(a - c + p2, __ldg(&tw[i][s + j]), p);
+// What every butterfly of a transform reads: the primes and the level tables of its length,
+// copied to shared memory once per work item.
+struct StageConst {
+    uint32_t p[kPrimes];
+    const uint2 *tw[kPrimes];
+};
+
+// np prime groups of 2^lnl interleaved transforms of length 2^ln; element e of transform l of
+// group i sits at buf[(i << lgs) + l + (e << lst)].  All index arithmetic is shifts and masks.
+struct Shape {
+    int ln, lnl, lst, lgs, np;
+};
+
+__device__ __forceinline__ void load_const(StageConst *K, const Desc &D, const uint2 *const *tw) {
+    if (threadIdx.x < kPrimes) {
+        K->p[threadIdx.x] = D.pr[threadIdx.x].p;
+        K->tw[threadIdx.x] = tw[threadIdx.x];
     }
 }
 
-// Inverse DIT stage of half-size s: (a, b) -> (a + b w, a - b w), w = w_2s^-j.
-__device__ __forceinline__ void dit_stage(uint32_t *buf, int n, int s, int nl, int stride_l, int st,
-                                          const Desc &D, const uint2 *const *tw, int nprime_groups,
-                                          int group_stride) {
-    const int half = n / 2;
-    const int total = nprime_groups * nl * half;
+// DIF levels of half-size s = 2^ls and s/2 in one radix-4 butterfly (ls >= 1):
+//   level s:   (x0, x2) -> (x0 + x2, (x0 - x2) w_2s^j),   (x1, x3) -> (.., (x1 - x3) w_2s^(j+s/2))
+//   level s/2: (a0, a1) -> (a0 + a1, (a0 - a1) w_s^j),   (a2, a3) likewise
+// with x0..x3 at i0, i0 + s/2, i0 + s, i0 + 3s/2.  Inputs and outputs in [0, 2p).
+__device__ __forceinline__ void dif4(uint32_t *buf, const Shape &S, int ls, const StageConst &K) {
+    const int lq = S.ln - 2, total = S.np << (S.lnl + lq);
+    const int s = 1 << ls, h = s >> 1;
     for (int q = threadIdx.x; q < total; q += blockDim.x) {
-        const int l = q % nl;
-        const int t = q / nl;
-        const int b = t % half, i = t / half;
-        const int j = b % s, i0 = (b / s) * 2 * s + j;
-        uint32_t *base = buf + i * group_stride + l * stride_l;
-        const uint32_t p = D.pr[i].p, p2 = 2 * p;
-        const uint32_t a = base[i0 * st];
-        const uint32_t c = shoup(base[(i0 + s) * st], __ldg(&tw[i][s + j]), p);
-        base[i0 * st] = red2(a + c, p2);
-        base[(i0 + s) * st] = red2(a - c + p2, p2);
+        const int l = q & ((1 << S.lnl) - 1), t = q >> S.lnl;
+        const int b = t & ((1 << lq) - 1), i = t >> lq;
+        const int j = b & (h - 1), i0 = ((b >> (ls - 1)) << (ls + 1)) + j;
+        uint32_t *e = buf + (i << S.lgs) + l;
+        const int st = S.lst;
+        const uint32_t p = K.p[i], p2 = 2 * p;
+        const uint2 *tw = K.tw[i];
+        const uint32_t x0 = e[i0 << st], x1 = e[(i0 + h) << st], x2 = e[(i0 + s) << st], x3 = e[(i0 + s + h) << st];
+        const uint32_t a0 = red2(x0 + x2, p2), a2 = shoup(x0 - x2 + p2, __ldg(&tw[s + j]), p);
+        const uint32_t a1 = red2(x1 + x3, p2), a3 = shoup(x1 - x3 + p2, __ldg(&tw[s + h + j]), p);
+        const uint2 w = __ldg(&tw[h + j]);
+        e[i0 << st] = red2(a0 + a1, p2);
+        e[(i0 + h) << st] = shoup(a0 - a1 + p2, w, p);
+        e[(i0 + s) << st] = red2(a2 + a3, p2);
+        e[(i0 + s + h) << st] = shoup(a2 - a3 + p2, w, p);
     }
 }
+
+// the last DIF level (s = 1, twiddle 1) when the length is an odd power of 2
+__device__ __forceinline__ void dif2_last(uint32_t *buf, const Shape &S, const StageConst &K) {
+    const int lq = S.ln - 1, total = S.np << (S.lnl + lq);
+    for (int q = threadIdx.x; q < total; q += blockDim.x) {
+        const int l = q & ((1 << S.lnl) - 1), t = q >> S.lnl;
+        const int b = t & ((1 << lq) - 1), i = t >> lq;
+        uint32_t *e = buf + (i << S.lgs) + l;
+        const int st = S.lst;
+        const uint32_t p2 = 2 * K.p[i];
+        const uint32_t x0 = e[(2 * b) << st], x1 = e[(2 * b + 1) << st];
+        e[(2 * b) << st] = red2(x0 + x1, p2);
+        e[(2 * b + 1) << st] = red2(x0 - x1 + p2, p2);
+    }
+}
+
+// DIT levels of half-size s = 2^ls and 2s in one radix-4 butterfly, on x0..x3 at i0 + {0,1,2,3}s:
+//   level s:  (x0, x1) -> (x0 + c, x0 - c), c = x1 w_2s^-j;  (x2, x3) likewise
+//   level 2s: (y0, y2) with w_4s^-j, (y1, y3) with w_4s^-(j+s)
+__device__ __forceinline__ void dit4(uint32_t *buf, const Shape &S, int ls, const StageConst &K) {
+    const int lq = S.ln - 2, total = S.np << (S.lnl + lq);
+    const int s = 1 << ls;
+    for (int q = threadIdx.x; q < total; q += blockDim.x) {
+        const int l = q & ((1 << S.lnl) - 1), t = q >> S.lnl;
+        const int b = t & ((1 << lq) - 1), i = t >> lq;
+        const int j = b & (s - 1), i0 = ((b >> ls) << (ls + 2)) + j;
+        uint32_t *e = buf + (i << S.lgs) + l;
+        const int st = S.lst;
+        const uint32_t p = K.p[i], p2 = 2 * p;
+        const uint2 *tw = K.tw[i];
+        const uint2 w1 = __ldg(&tw[s + j]);
+        const uint32_t x0 = e[i0 << st], x1 = shoup(e[(i0 + s) << st], w1, p);
+        const uint32_t x2 = e[(i0 + 2 * s) << st], x3 = shoup(e[(i0 + 3 * s) << st], w1, p);
+        const uint32_t y0 = red2(x0 + x1, p2), y1 = red2(x0 - x1 + p2, p2);
+        const uint32_t y2 = shoup(red2(x2 + x3, p2), __ldg(&tw[2 * s + j]), p);
+        const uint32_t y3 = shoup(red2(x2 - x3 + p2, p2), __ldg(&tw[3 * s + j]), p);
+        e[i0 << st] = red2(y0 + y2, p2);
+        e[(i0 + 2 * s) << st] = red2(y0 - y2 + p2, p2);
+        e[(i0 + s) << st] = red2(y1 + y3, p2);
+        e[(i0 + 3 * s) << st] = red2(y1 - y3 + p2, p2);
+    }
+}
+
+// the last DIT level (s = n/2) when the length is an odd power of 2
+__device__ __forceinline__ void dit2_last(uint32_t *buf, const Shape &S, const StageConst &K) {
+    const int lq = S.ln - 1, total = S.np << (S.lnl + lq);
+    const int s = 1 << lq;
+    for (int q = threadIdx.x; q < total; q += blockDim.x) {
+        const int l = q & ((1 << S.lnl) - 1), t = q >> S.lnl;
+        const int j = t & (s - 1), i = t >> lq;
+        uint32_t *e = buf + (i << S.lgs) + l;
+        const int st = S.lst;
+        const uint32_t p = K.p[i], p2 = 2 * p;
+        const uint32_t a = e[j << st], c = shoup(e[(j + s) << st], __ldg(&K.tw[i][s + j]), p);
+        e[j << st] = red2(a + c, p2);
+        e[(j + s) << st] = red2(a - c + p2, p2);
+    }
+}
+
+// forward transform (natural order in, bit-reversed out); ends with a barrier
+__device__ __forceinline__ void ntt_forward(uint32_t *buf, const Shape &S, const StageConst &K) {
+    int ls = S.ln - 1;
+    for (; ls >= 1; ls -= 2) {
+        dif4(buf, S, ls, K);
+        __syncthreads();
+    }
+    if (ls == 0) {
+        dif2_last(buf, S, K);
+        __syncthreads();
+    }
+}
+
+// inverse transform (bit-reversed in, natural out, unscaled); ends with a barrier
+__device__ __forceinline__ void ntt_inverse(uint32_t *buf, const Shape &S, const StageConst &K) {
+    int ls = 0;
+    for (; ls + 1 <= S.ln - 1; ls += 2) {
+        dit4(buf, S, ls, K);
+        __syncthreads();
+    }
+    if (ls == S.ln - 1) {
+        dit2_last(buf, S, K);
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ int log2i(uint32_t x) { return 31 - __clz(x); }
 
 // ---- pass kernels -----------------------------------------------------------------------------
 
@@ -146,12 +238,14 @@ __device__ __forceinline__ void dit_stage(uint32_t *buf, int n, int s, int nl, i
 __global__ void __launch_bounds__(kColThreads) kn_col_fwd(const Desc *descs, const int2 *items, int nitems,
                                                           int second, const uint64_t *src_o) {
     extern __shared__ uint32_t sm[];
+    __shared__ StageConst K;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const int2 wi = items[it];
         const Desc &D = descs[wi.x];
         const int R = (int)D.R, C = (int)D.C, g = wi.y;
         const uint64_t *src = src_o ? src_o : (second ? D.y : D.x);
         uint32_t *dst = second ? D.res2 : D.res;
+        load_const(&K, D, D.tb.twr_f);
         for (int e = threadIdx.x; e < R * kG; e += blockDim.x) {
             const int r = e / kG, l = e % kG;
             const uint32_t j = (uint32_t)r * C + g * kG + l;
@@ -160,10 +254,8 @@ __global__ void __launch_bounds__(kColThreads) kn_col_fwd(const Desc *descs, con
             for (int i = 0; i < kPrimes; i++) sm[(i * R + r) * kG + l] = residue(word, D.pr[i]);
         }
         __syncthreads();
-        for (int s = R / 2; s >= 1; s >>= 1) {
-            dif_stage(sm, R, s, kG, 1, kG, D, D.tb.twr_f, kPrimes, R * kG);
-            __syncthreads();
-        }
+        const int lR = log2i(R);
+        ntt_forward(sm, Shape{lR, 3, 3, lR + 3, kPrimes}, K);
         for (int e = threadIdx.x; e < kPrimes * R * kG; e += blockDim.x) {
             const int l = e % kG, t = e / kG, pos = t % R, i = t / R;
             const uint32_t m = (uint32_t)pos * C + g * kG + l;
@@ -177,36 +269,32 @@ __global__ void __launch_bounds__(kColThreads) kn_col_fwd(const Desc *descs, con
 template <bool MUL>
 __global__ void __launch_bounds__(kRowThreads) kn_rows(const Desc *descs, const int2 *items, int nitems) {
     extern __shared__ uint32_t sm[];
+    __shared__ StageConst Kf, Ki;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const int2 wi = items[it];
         const Desc &D = descs[wi.x];
         const int C = (int)D.C, pos = wi.y;
+        load_const(&Kf, D, D.tb.twc_f);
+        load_const(&Ki, D, D.tb.twc_i);
         for (int e = threadIdx.x; e < kPrimes * C; e += blockDim.x) {
-            const int i = e / C, c = e % C;
-            const size_t m = (size_t)i * D.NP + (size_t)pos * C + c;
-            sm[i * C + c] = D.res[m];
-            if (MUL) sm[(kPrimes + i) * C + c] = D.res2[m];
+            const size_t m = (size_t)(e / C) * D.NP + (size_t)pos * C + (e % C);
+            sm[e] = D.res[m];
+            if (MUL) sm[kPrimes * C + e] = D.res2[m];
         }
         __syncthreads();
-        for (int s = C / 2; s >= 1; s >>= 1) {
-            dif_stage(sm, C, s, 1, 0, 1, D, D.tb.twc_f, kPrimes, C);
-            if (MUL) dif_stage(sm + kPrimes * C, C, s, 1, 0, 1, D, D.tb.twc_f, kPrimes, C);
-            __syncthreads();
-        }
+        const int lC = log2i(C);
+        const Shape S{lC, 0, 0, lC, kPrimes};
+        ntt_forward(sm, S, Kf);
+        if (MUL) ntt_forward(sm + kPrimes * C, S, Kf);
         for (int e = threadIdx.x; e < kPrimes * C; e += blockDim.x) {
-            const int i = e / C;
+            const int i = e >> lC;
             const uint32_t a = sm[e];
             sm[e] = montmul(a, MUL ? sm[kPrimes * C + e] : a, D.pr[i].p, D.pr[i].pinv);
         }
         __syncthreads();
-        for (int s = 1; s < C; s <<= 1) {
-            dit_stage(sm, C, s, 1, 0, 1, D, D.tb.twc_i, kPrimes, C);
-            __syncthreads();
-        }
-        for (int e = threadIdx.x; e < kPrimes * C; e += blockDim.x) {
-            const int i = e / C, c = e % C;
-            D.res[(size_t)i * D.NP + (size_t)pos * C + c] = sm[i * C + c];
-        }
+        ntt_inverse(sm, S, Ki);
+        for (int e = threadIdx.x; e < kPrimes * C; e += blockDim.x)
+            D.res[(size_t)(e >> lC) * D.NP + (size_t)pos * C + (e & (C - 1))] = sm[e];
         __syncthreads();
     }
 }
@@ -233,20 +321,20 @@ __device__ __forceinline__ ulonglong2 garner(const uint32_t *v, const Desc &D) {
 
 __global__ void __launch_bounds__(kColThreads) kn_col_inv(const Desc *descs, const int2 *items, int nitems) {
     extern __shared__ uint32_t sm[];
+    __shared__ StageConst K;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const int2 wi = items[it];
         const Desc &D = descs[wi.x];
         const int R = (int)D.R, C = (int)D.C, g = wi.y;
+        load_const(&K, D, D.tb.twr_i);
         for (int e = threadIdx.x; e < kPrimes * R * kG; e += blockDim.x) {
             const int l = e % kG, t = e / kG, pos = t % R, i = t / R;
             const uint32_t m = (uint32_t)pos * C + g * kG + l;
             sm[(i * R + pos) * kG + l] = shoup(D.res[(size_t)i * D.NP + m], __ldg(&D.tb.t4_i[i][m]), D.pr[i].p);
         }
         __syncthreads();
-        for (int s = 1; s < R; s <<= 1) {
-            dit_stage(sm, R, s, kG, 1, kG, D, D.tb.twr_i, kPrimes, R * kG);
-            __syncthreads();
-        }
+        const int lR = log2i(R);
+        ntt_inverse(sm, Shape{lR, 3, 3, lR + 3, kPrimes}, K);
         for (int e = threadIdx.x; e < R * kG; e += blockDim.x) {
             const int r = e / kG, l = e % kG;
             const uint32_t j = (uint32_t)r * C + g * kG + l;
@@ -693,6 +781,28 @@ void choose_sizes(uint64_t k, uint64_t n, uint32_t &w, uint32_t &W, uint32_t &NP
     NP = best_np;
 }
 
+// The dynamic shared-memory limit is a per-kernel property of the device's context, shared by
+// every engine and group of the process: raise it, never lower it, so a small engine created
+// later cannot break a larger group's captured launches.
+bool prepare_smem(int device, size_t col_smem, size_t row_smem) {
+    static std::mutex mu;
+    static size_t col_hw[64] = {}, row_hw[64] = {};
+    if (device < 0 || device >= 64) return false;
+    std::lock_guard<std::mutex> lock(mu);
+    bool ok = true;
+    if (col_smem > col_hw[device]) {
+        ok = ok && cudaFuncSetAttribute(kn_col_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)col_smem) == cudaSuccess;
+        ok = ok && cudaFuncSetAttribute(kn_col_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)col_smem) == cudaSuccess;
+        if (ok) col_hw[device] = col_smem;
+    }
+    if (row_smem > row_hw[device]) {
+        ok = ok && cudaFuncSetAttribute(kn_rows<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)row_smem) == cudaSuccess;
+        ok = ok && cudaFuncSetAttribute(kn_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)row_smem) == cudaSuccess;
+        if (ok) row_hw[device] = row_smem;
+    }
+    return ok;
+}
+
 }  // namespace
 
 extern "C" {
@@ -740,13 +850,7 @@ kn_engine *kn_engine_new(uint64_t k, uint64_t n, int device) {
              kok(e, cudaMemcpy(e->d_test, &zero, sizeof zero, cudaMemcpyHostToDevice)) &&
              kok(e, cudaMemcpy(e->d_status, &zero, sizeof zero, cudaMemcpyHostToDevice));
     }
-    if (ok) {
-        const size_t col_smem = (size_t)kPrimes * R * kG * 4, row_smem = (size_t)2 * kPrimes * C * 4;
-        ok = kok(e, cudaFuncSetAttribute(kn_col_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)col_smem)) &&
-             kok(e, cudaFuncSetAttribute(kn_col_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)col_smem)) &&
-             kok(e, cudaFuncSetAttribute(kn_rows<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)row_smem)) &&
-             kok(e, cudaFuncSetAttribute(kn_rows<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)row_smem));
-    }
+    if (ok) ok = prepare_smem(device, (size_t)kPrimes * R * kG * 4, (size_t)2 * kPrimes * C * 4);
     if (!ok) {
         kn_engine_free(e);
         return nullptr;
@@ -927,5 +1031,171 @@ int kn_sync(kn_engine *e) {
     kok(e, cudaStreamSynchronize(e->stream));
     return e->err;
 }
+
+
+// ---- groups: many tests squared by one launch set per squaring ---------------------------------
+
+struct kn_group {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<kn_engine *> eng;
+    std::vector<uint64_t *> xs;
+    Desc *d_desc = nullptr;
+    int2 *d_cols = nullptr, *d_rows = nullptr;
+    int *d_tests = nullptr;
+    int ncols = 0, nrows = 0, ntests = 0;
+    size_t col_smem = 0, row_smem = 0;
+    int grid = 0;
+    int threads = 128;  // block size of the transform kernels
+    bool dirty = true;
+    cudaGraphExec_t graph = nullptr;
+    uint32_t graph_len = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int err = 0;
+};
+
+namespace {
+
+bool gok(kn_group *g, cudaError_t c) {
+    if (c != cudaSuccess && !g->err) g->err = (int)c;
+    return c == cudaSuccess;
+}
+
+void group_free_lists(kn_group *g) {
+    for (void *p : {(void *)g->d_desc, (void *)g->d_cols, (void *)g->d_rows, (void *)g->d_tests})
+        if (p) cudaFree(p);
+    g->d_desc = nullptr;
+    g->d_cols = g->d_rows = nullptr;
+    g->d_tests = nullptr;
+    if (g->graph) cudaGraphExecDestroy(g->graph);
+    g->graph = nullptr;
+    g->graph_len = 0;
+}
+
+// descriptor table and work lists of the members, longest transforms first
+bool group_build(kn_group *g) {
+    if (!g->dirty) return true;
+    group_free_lists(g);
+    const int m = (int)g->eng.size();
+    std::vector<int> order(m);
+    for (int i = 0; i < m; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return g->eng[a]->NP > g->eng[b]->NP; });
+    std::vector<Desc> descs(m);
+    std::vector<int2> cols, rows;
+    std::vector<int> tests(m);
+    g->col_smem = g->row_smem = 0;
+    for (int t = 0; t < m; t++) {
+        kn_engine *e = g->eng[order[t]];
+        descs[t] = e->desc;
+        descs[t].x = g->xs[order[t]];
+        descs[t].addend = nullptr;
+        tests[t] = t;
+        for (uint32_t c = 0; c < e->plan->C / kG; c++) cols.push_back(make_int2(t, (int)c));
+        for (uint32_t r = 0; r < e->plan->R; r++) rows.push_back(make_int2(t, (int)r));
+        g->col_smem = std::max(g->col_smem, (size_t)kPrimes * e->plan->R * kG * 4);
+        g->row_smem = std::max(g->row_smem, (size_t)kPrimes * e->plan->C * 4);
+    }
+    g->ncols = (int)cols.size();
+    g->nrows = (int)rows.size();
+    g->ntests = m;
+    bool ok = gok(g, cudaMalloc((void **)&g->d_desc, m * sizeof(Desc))) &&
+              gok(g, cudaMalloc((void **)&g->d_cols, cols.size() * sizeof(int2))) &&
+              gok(g, cudaMalloc((void **)&g->d_rows, rows.size() * sizeof(int2))) &&
+              gok(g, cudaMalloc((void **)&g->d_tests, m * sizeof(int))) &&
+              gok(g, cudaMemcpy(g->d_desc, descs.data(), m * sizeof(Desc), cudaMemcpyHostToDevice)) &&
+              gok(g, cudaMemcpy(g->d_cols, cols.data(), cols.size() * sizeof(int2), cudaMemcpyHostToDevice)) &&
+              gok(g, cudaMemcpy(g->d_rows, rows.data(), rows.size() * sizeof(int2), cudaMemcpyHostToDevice)) &&
+              gok(g, cudaMemcpy(g->d_tests, tests.data(), m * sizeof(int), cudaMemcpyHostToDevice));
+    if (ok) ok = prepare_smem(g->device, g->col_smem, 2 * g->row_smem);
+    g->dirty = !ok;
+    return ok;
+}
+
+void group_square_once(kn_group *g) {
+    const int gc = std::min(g->ncols, g->grid), gr = std::min(g->nrows, g->grid);
+    kn_col_fwd<<<gc, g->threads, g->col_smem, g->stream>>>(g->d_desc, g->d_cols, g->ncols, 0, nullptr);
+    kn_rows<false><<<gr, g->threads, g->row_smem, g->stream>>>(g->d_desc, g->d_rows, g->nrows);
+    kn_col_inv<<<gc, g->threads, g->col_smem, g->stream>>>(g->d_desc, g->d_cols, g->ncols);
+    kn_reduce<<<g->ntests, kReduceThreads, 0, g->stream>>>(g->d_desc, g->d_tests, nullptr, nullptr);
+}
+
+constexpr uint32_t kGroupChunk = 8;  // squarings per captured graph
+
+}  // namespace
+
+kn_group *kn_group_new(int device) {
+    if (device < 0 && cudaGetDevice(&device) != cudaSuccess) return nullptr;
+    if (cudaSetDevice(device) != cudaSuccess) return nullptr;
+    kn_group *g = new (std::nothrow) kn_group();
+    if (!g) return nullptr;
+    g->device = device;
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    // 128-thread blocks, 16 per SM: on GB300 over 256 tests, 0.788 ms per squaring step against
+    // 0.818 ms with 256 threads and 0.837 ms with 64
+    g->threads = 128;
+    g->grid = std::max(1, nsm) * 16;
+    if (!gok(g, cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking)) || !gok(g, cudaEventCreate(&g->ev0)) ||
+        !gok(g, cudaEventCreate(&g->ev1))) {
+        kn_group_free(g);
+        return nullptr;
+    }
+    return g;
+}
+
+void kn_group_free(kn_group *g) {
+    if (!g) return;
+    cudaSetDevice(g->device);
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    group_free_lists(g);
+    if (g->ev0) cudaEventDestroy(g->ev0);
+    if (g->ev1) cudaEventDestroy(g->ev1);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+}
+
+int kn_group_add(kn_group *g, kn_engine *e, uint64_t *x) {
+    if (!g || !e || !x || g->err || e->device != g->device) return -1;
+    for (kn_engine *o : g->eng)
+        if (o == e) return -1;  // members own their engine's scratch
+    kn_sync(e);
+    g->eng.push_back(e);
+    g->xs.push_back(x);
+    g->dirty = true;
+    return (int)g->eng.size() - 1;
+}
+
+int kn_group_square(kn_group *g, uint64_t count, float *gpu_ms) {
+    if (!g || g->err) return -1;
+    if (g->eng.empty() || !count) return 0;
+    cudaSetDevice(g->device);
+    if (!group_build(g)) return -1;
+    if (!g->graph) {
+        cudaGraph_t graph = nullptr;
+        if (!gok(g, cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal))) return -1;
+        for (uint32_t i = 0; i < kGroupChunk; i++) group_square_once(g);
+        if (!gok(g, cudaStreamEndCapture(g->stream, &graph))) return -1;
+        const bool ok = gok(g, cudaGraphInstantiate(&g->graph, graph, 0));
+        cudaGraphDestroy(graph);
+        if (!ok) return -1;
+        g->graph_len = kGroupChunk;
+    }
+    gok(g, cudaEventRecord(g->ev0, g->stream));
+    uint64_t done = 0;
+    for (; done + g->graph_len <= count; done += g->graph_len)
+        if (!gok(g, cudaGraphLaunch(g->graph, g->stream))) return -1;
+    for (; done < count; done++) group_square_once(g);
+    gok(g, cudaEventRecord(g->ev1, g->stream));
+    if (!gok(g, cudaGetLastError()) || !gok(g, cudaStreamSynchronize(g->stream))) return -1;
+    if (gpu_ms) cudaEventElapsedTime(gpu_ms, g->ev0, g->ev1);
+    for (kn_engine *e : g->eng) {
+        int st = 0;
+        cudaMemcpy(&st, e->d_status, sizeof st, cudaMemcpyDeviceToHost);
+        if (st) g->err = -100 - st;
+    }
+    return g->err ? -1 : 0;
+}
+
+int kn_group_error(const kn_group *g) { return g ? g->err : -1; }
 
 }  // extern "C"

@@ -190,6 +190,11 @@ PROTOTYPES = {
     "kn_copy": (C.c_int, [vp, vp, vp]),
     "kn_error": (C.c_int, [vp]),
     "kn_sync": (C.c_int, [vp]),
+    "kn_group_new": (vp, [C.c_int]),
+    "kn_group_free": (None, [vp]),
+    "kn_group_add": (C.c_int, [vp, vp, vp]),
+    "kn_group_square": (C.c_int, [vp, C.c_uint64, C.POINTER(C.c_float)]),
+    "kn_group_error": (C.c_int, [vp]),
     # PRST-compatible proofs (include/kite_proof.h)
     "pp_giant_free": (None, [C.POINTER(PpGiant)]),
     "pp_fingerprint": (C.c_uint32, [C.c_uint64, C.c_uint64]),

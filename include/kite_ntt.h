@@ -57,6 +57,18 @@ int kn_copy(kn_engine *e, uint64_t *dst, const uint64_t *src);
 int kn_error(const kn_engine *e);
 int kn_sync(kn_engine *e);
 
+/* Groups: one launch set per squaring advances every member at once (many tests on one GPU, as
+ * the reference's prototype keeps B numbers in flight, gpu/gpu_ctx.h:57-77).  A member is an
+ * engine with the number it squares; engines may differ in k and n but not repeat, since each
+ * owns its scratch.  Squarings run as CUDA graphs of 8.  gpu_ms (optional) receives the GPU time
+ * of the call, measured with events on the group's stream. */
+typedef struct kn_group kn_group;
+kn_group *kn_group_new(int device);
+void kn_group_free(kn_group *g);
+int kn_group_add(kn_group *g, kn_engine *e, uint64_t *x);
+int kn_group_square(kn_group *g, uint64_t count, float *gpu_ms);
+int kn_group_error(const kn_group *g);
+
 #ifdef __cplusplus
 }
 #endif

@@ -170,3 +170,31 @@ def test_cross_check_with_fp64_engine(lib):
         assert e.get(x) == v_fp
     finally:
         e.close()
+
+
+def test_group_squares_every_member(lib):
+    """a group of tests with different k, n and transform lengths: graph chunks plus a remainder,
+    every member exact"""
+    from ahnum_gb300 import native
+    sizes = [(3, 1000), (9357, 20000), (1203, 90001), (4733, 369717), (7, 7)]
+    engines = [Engine(k, n) for k, n in sizes if n >= 8]
+    g = lib.kn_group_new(-1)
+    assert g
+    try:
+        xs, want = [], []
+        for i, e in enumerate(engines):
+            v = _seeded_residue(200 + i, e.k, e.n)
+            x = e.num(v)
+            xs.append(x)
+            want.append(pow(v, 1 << 21, e.N))
+            assert lib.kn_group_add(g, e.h, x) == i
+        assert lib.kn_group_add(g, engines[0].h, xs[0]) == -1  # an engine joins once
+        ms = C.c_float(0)
+        assert lib.kn_group_square(g, 21, C.byref(ms)) == 0
+        assert ms.value > 0
+        for e, x, w in zip(engines, xs, want):
+            assert e.get(x) == w
+    finally:
+        lib.kn_group_free(g)
+        for e in engines:
+            e.close()
