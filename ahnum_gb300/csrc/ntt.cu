@@ -7,8 +7,10 @@
 //   kn_rows      per row: forward row NTT (DIF), pointwise Montgomery square or product,
 //                inverse row NTT (decimation in time, bit-reversed in, natural out).
 //   kn_col_inv   per column group: times w_NP^(-k_r c) 2^32 / NP, inverse column NTT (DIT),
-//                Garner CRT of the four residues into the exact coefficient (< 2^120).
-//   kn_reduce    per test, one block: carry the coefficients into words of P = x^2, Montgomery
+//                Garner CRT of the four residues into the exact coefficients (< 2^120), and the
+//                carry through each row's 8 consecutive coefficients: 8 words of the product P
+//                and one segment carry.
+//   kn_reduce    per test, one block: the segment carries into the words of P = x^2, Montgomery
 //                reduction P 2^-n == B + k A (mod N) for P = A + B 2^n, A < 2^n, plus an
 //                optional constant, carry, and the top fold T 2^n == q + r 2^n for T = q k + r.
 // Reference: gpu/ntt_reg.metal:90-246 (the four-step NTT passes), gpu/sq.metal:23-192 (residues,
@@ -43,7 +45,7 @@ constexpr uint32_t kP[kPrimes] = {1053818881u, 975175681u, 943718401u, 880803841
 constexpr int kG = 8;                // columns per column group
 constexpr int kColThreads = 256;
 constexpr int kRowThreads = 256;
-constexpr int kReduceThreads = 512;
+constexpr int kReduceThreads = 256;
 
 struct Prime {
     uint32_t p;
@@ -64,13 +66,13 @@ struct Crt {
 };
 
 struct Desc {
-    uint32_t NP, R, C, NU;      // NU: coefficients that can be non-zero (2W - 1, rounded up)
+    uint32_t NP, R, C;
     uint32_t W, w, WN0, BN0;    // words, word bits, n / w, n % w
     uint64_t k;
     uint64_t *x;                // operand and result
     const uint64_t *y;          // second operand of a product
     uint32_t *res, *res2;       // 4 NP residues each
-    ulonglong2 *coef;           // NP exact coefficients (lo, hi)
+    ulonglong2 *seg;            // NP / 8 carries out of the product's 8-word segments (lo, hi)
     uint64_t *pw;               // NP words of the product
     const uint64_t *addend;     // W words added after the reduction, or null
     int *status;                // non-zero: a carry left the number (cannot happen for valid input)
@@ -99,203 +101,200 @@ __device__ __forceinline__ uint32_t residue(uint64_t word, const Prime &P) {
     return red2(shoup(lo, P.one, P.p) + shoup(hi, P.r32, P.p), 2 * P.p);
 }
 
-// What every butterfly of a transform reads: the primes and the level tables of its length,
-// copied to shared memory once per work item.
-struct StageConst {
-    uint32_t p[kPrimes];
-    const uint2 *tw[kPrimes];
-};
-
-// np prime groups of 2^lnl interleaved transforms of length 2^ln; element e of transform l of
-// group i sits at buf[(i << lgs) + l + (e << lst)].  All index arithmetic is shifts and masks.
-struct Shape {
-    int ln, lnl, lst, lgs, np;
-};
-
-__device__ __forceinline__ void load_const(StageConst *K, const Desc &D, const uint2 *const *tw) {
-    if (threadIdx.x < kPrimes) {
-        K->p[threadIdx.x] = D.pr[threadIdx.x].p;
-        K->tw[threadIdx.x] = tw[threadIdx.x];
-    }
-}
-
-// DIF levels of half-size s = 2^ls and s/2 in one radix-4 butterfly (ls >= 1):
-//   level s:   (x0, x2) -> (x0 + x2, (x0 - x2) w_2s^j),   (x1, x3) -> (.., (x1 - x3) w_2s^(j+s/2))
-//   level s/2: (a0, a1) -> (a0 + a1, (a0 - a1) w_s^j),   (a2, a3) likewise
-// with x0..x3 at i0, i0 + s/2, i0 + s, i0 + 3s/2.  Inputs and outputs in [0, 2p).
-__device__ __forceinline__ void dif4(uint32_t *buf, const Shape &S, int ls, const StageConst &K) {
-    const int lq = S.ln - 2, total = S.np << (S.lnl + lq);
-    const int s = 1 << ls, h = s >> 1;
-    for (int q = threadIdx.x; q < total; q += blockDim.x) {
-        const int l = q & ((1 << S.lnl) - 1), t = q >> S.lnl;
-        const int b = t & ((1 << lq) - 1), i = t >> lq;
-        const int j = b & (h - 1), i0 = ((b >> (ls - 1)) << (ls + 1)) + j;
-        uint32_t *e = buf + (i << S.lgs) + l;
-        const int st = S.lst;
-        const uint32_t p = K.p[i], p2 = 2 * p;
-        const uint2 *tw = K.tw[i];
-        const uint32_t x0 = e[i0 << st], x1 = e[(i0 + h) << st], x2 = e[(i0 + s) << st], x3 = e[(i0 + s + h) << st];
-        const uint32_t a0 = red2(x0 + x2, p2), a2 = shoup(x0 - x2 + p2, __ldg(&tw[s + j]), p);
-        const uint32_t a1 = red2(x1 + x3, p2), a3 = shoup(x1 - x3 + p2, __ldg(&tw[s + h + j]), p);
-        const uint2 w = __ldg(&tw[h + j]);
-        e[i0 << st] = red2(a0 + a1, p2);
-        e[(i0 + h) << st] = shoup(a0 - a1 + p2, w, p);
-        e[(i0 + s) << st] = red2(a2 + a3, p2);
-        e[(i0 + s + h) << st] = shoup(a2 - a3 + p2, w, p);
-    }
-}
-
-// the last DIF level (s = 1, twiddle 1) when the length is an odd power of 2
-__device__ __forceinline__ void dif2_last(uint32_t *buf, const Shape &S, const StageConst &K) {
-    const int lq = S.ln - 1, total = S.np << (S.lnl + lq);
-    for (int q = threadIdx.x; q < total; q += blockDim.x) {
-        const int l = q & ((1 << S.lnl) - 1), t = q >> S.lnl;
-        const int b = t & ((1 << lq) - 1), i = t >> lq;
-        uint32_t *e = buf + (i << S.lgs) + l;
-        const int st = S.lst;
-        const uint32_t p2 = 2 * K.p[i];
-        const uint32_t x0 = e[(2 * b) << st], x1 = e[(2 * b + 1) << st];
-        e[(2 * b) << st] = red2(x0 + x1, p2);
-        e[(2 * b + 1) << st] = red2(x0 - x1 + p2, p2);
-    }
-}
-
-// DIT levels of half-size s = 2^ls and 2s in one radix-4 butterfly, on x0..x3 at i0 + {0,1,2,3}s:
-//   level s:  (x0, x1) -> (x0 + c, x0 - c), c = x1 w_2s^-j;  (x2, x3) likewise
-//   level 2s: (y0, y2) with w_4s^-j, (y1, y3) with w_4s^-(j+s)
-__device__ __forceinline__ void dit4(uint32_t *buf, const Shape &S, int ls, const StageConst &K) {
-    const int lq = S.ln - 2, total = S.np << (S.lnl + lq);
-    const int s = 1 << ls;
-    for (int q = threadIdx.x; q < total; q += blockDim.x) {
-        const int l = q & ((1 << S.lnl) - 1), t = q >> S.lnl;
-        const int b = t & ((1 << lq) - 1), i = t >> lq;
-        const int j = b & (s - 1), i0 = ((b >> ls) << (ls + 2)) + j;
-        uint32_t *e = buf + (i << S.lgs) + l;
-        const int st = S.lst;
-        const uint32_t p = K.p[i], p2 = 2 * p;
-        const uint2 *tw = K.tw[i];
-        const uint2 w1 = __ldg(&tw[s + j]);
-        const uint32_t x0 = e[i0 << st], x1 = shoup(e[(i0 + s) << st], w1, p);
-        const uint32_t x2 = e[(i0 + 2 * s) << st], x3 = shoup(e[(i0 + 3 * s) << st], w1, p);
-        const uint32_t y0 = red2(x0 + x1, p2), y1 = red2(x0 - x1 + p2, p2);
-        const uint32_t y2 = shoup(red2(x2 + x3, p2), __ldg(&tw[2 * s + j]), p);
-        const uint32_t y3 = shoup(red2(x2 - x3 + p2, p2), __ldg(&tw[3 * s + j]), p);
-        e[i0 << st] = red2(y0 + y2, p2);
-        e[(i0 + 2 * s) << st] = red2(y0 - y2 + p2, p2);
-        e[(i0 + s) << st] = red2(y1 + y3, p2);
-        e[(i0 + 3 * s) << st] = red2(y1 - y3 + p2, p2);
-    }
-}
-
-// the last DIT level (s = n/2) when the length is an odd power of 2
-__device__ __forceinline__ void dit2_last(uint32_t *buf, const Shape &S, const StageConst &K) {
-    const int lq = S.ln - 1, total = S.np << (S.lnl + lq);
-    const int s = 1 << lq;
-    for (int q = threadIdx.x; q < total; q += blockDim.x) {
-        const int l = q & ((1 << S.lnl) - 1), t = q >> S.lnl;
-        const int j = t & (s - 1), i = t >> lq;
-        uint32_t *e = buf + (i << S.lgs) + l;
-        const int st = S.lst;
-        const uint32_t p = K.p[i], p2 = 2 * p;
-        const uint32_t a = e[j << st], c = shoup(e[(j + s) << st], __ldg(&K.tw[i][s + j]), p);
-        e[j << st] = red2(a + c, p2);
-        e[(j + s) << st] = red2(a - c + p2, p2);
-    }
-}
-
-// forward transform (natural order in, bit-reversed out); ends with a barrier
-__device__ __forceinline__ void ntt_forward(uint32_t *buf, const Shape &S, const StageConst &K) {
-    int ls = S.ln - 1;
-    for (; ls >= 1; ls -= 2) {
-        dif4(buf, S, ls, K);
-        __syncthreads();
-    }
-    if (ls == 0) {
-        dif2_last(buf, S, K);
-        __syncthreads();
-    }
-}
-
-// inverse transform (bit-reversed in, natural out, unscaled); ends with a barrier
-__device__ __forceinline__ void ntt_inverse(uint32_t *buf, const Shape &S, const StageConst &K) {
-    int ls = 0;
-    for (; ls + 1 <= S.ln - 1; ls += 2) {
-        dit4(buf, S, ls, K);
-        __syncthreads();
-    }
-    if (ls == S.ln - 1) {
-        dit2_last(buf, S, K);
-        __syncthreads();
-    }
-}
-
 __device__ __forceinline__ int log2i(uint32_t x) { return 31 - __clz(x); }
+
+// A length n = A*B transform runs as two register passes (Bailey's split of the levels):
+//   the "wide" levels, half-sizes n/2 .. B, pair elements B apart: a unit holds the A values at
+//   t + B m (m < A) for one t < B;
+//   the "narrow" levels, half-sizes B/2 .. 1, stay inside blocks of B consecutive elements: a
+//   unit holds one block, B t2 + m (m < B).
+// Between the passes the values go through shared memory once, with element e stored at
+// e + (e >> log2 B) so that both access patterns are free of bank conflicts.
+//
+// DIF levels over register values at positions c0 + m*stride: level s pairs m with m + s/stride
+// and multiplies the difference by w_2s^(c mod s) = tw[s + (c mod s)].
+template <int A>
+__device__ __forceinline__ void dif_regs(uint32_t (&x)[A], int c0, int stride, const uint2 *tw, uint32_t p) {
+    const uint32_t p2 = 2 * p;
+#pragma unroll
+    for (int half = A / 2; half >= 1; half >>= 1) {
+        const int s = stride * half;
+#pragma unroll
+        for (int m = 0; m < A; m++) {
+            if (m & half) continue;
+            const int c = c0 + m * stride;
+            const uint32_t u = x[m], v = x[m + half];
+            x[m] = red2(u + v, p2);
+            x[m + half] = shoup(u - v + p2, __ldg(&tw[s + (c & (s - 1))]), p);
+        }
+    }
+}
+
+// DIT levels (inverse), ascending: (u, v) -> (u + v w, u - v w), w = w_2s^-(c mod s)
+template <int A>
+__device__ __forceinline__ void dit_regs(uint32_t (&x)[A], int c0, int stride, const uint2 *tw, uint32_t p) {
+    const uint32_t p2 = 2 * p;
+#pragma unroll
+    for (int half = 1; half < A; half <<= 1) {
+        const int s = stride * half;
+#pragma unroll
+        for (int m = 0; m < A; m++) {
+            if (m & half) continue;
+            const int c = c0 + m * stride;
+            const uint32_t u = x[m], v = shoup(x[m + half], __ldg(&tw[s + (c & (s - 1))]), p);
+            x[m] = red2(u + v, p2);
+            x[m + half] = red2(u - v + p2, p2);
+        }
+    }
+}
+
+template <int X>
+__host__ __device__ constexpr int clog2() { return X <= 1 ? 0 : 1 + clog2<X / 2>(); }
 
 // ---- pass kernels -----------------------------------------------------------------------------
 
-// shared memory [prime][r][l], l < kG
+// Column layout in shared memory: [prime][padded r][l], l < kG.
+template <int B>
+__device__ __forceinline__ int col_addr(int i, int rp_len, int e, int l) {
+    return ((i * rp_len + e + (e >> clog2<B>())) << 3) + l;
+}
+
+template <int A, int B>
+__device__ __forceinline__ void col_fwd_item(uint32_t *sm, const Desc &D, int g, const uint64_t *src, uint32_t *dst) {
+    constexpr int R = A * B, RP = R + R / B;
+    const int C = (int)D.C;
+    for (int e = threadIdx.x; e < R * kG; e += blockDim.x) {
+        const int r = e >> 3, l = e & 7;
+        const uint32_t j = (uint32_t)r * C + g * kG + l;
+        const uint64_t word = j < D.W ? src[j] : 0;
+#pragma unroll
+        for (int i = 0; i < kPrimes; i++) sm[col_addr<B>(i, RP, r, l)] = residue(word, D.pr[i]);
+    }
+    __syncthreads();
+    for (int u = threadIdx.x; u < kPrimes * B * kG; u += blockDim.x) {
+        const int l = u & 7, t = (u >> 3) & (B - 1), i = u >> (3 + clog2<B>());
+        uint32_t x[A];
+#pragma unroll
+        for (int m = 0; m < A; m++) x[m] = sm[col_addr<B>(i, RP, t + B * m, l)];
+        dif_regs<A>(x, t, B, D.tb.twr_f[i], D.pr[i].p);
+#pragma unroll
+        for (int m = 0; m < A; m++) sm[col_addr<B>(i, RP, t + B * m, l)] = x[m];
+    }
+    __syncthreads();
+    for (int u = threadIdx.x; u < kPrimes * A * kG; u += blockDim.x) {
+        const int l = u & 7, t2 = (u >> 3) & (A - 1), i = u >> (3 + clog2<A>());
+        uint32_t x[B];
+#pragma unroll
+        for (int m = 0; m < B; m++) x[m] = sm[col_addr<B>(i, RP, B * t2 + m, l)];
+        dif_regs<B>(x, B * t2, 1, D.tb.twr_f[i], D.pr[i].p);
+        const uint32_t p = D.pr[i].p;
+#pragma unroll
+        for (int m = 0; m < B; m++) {
+            const uint32_t mm = (uint32_t)(B * t2 + m) * C + g * kG + l;  // storage position B t2 + m
+            dst[(size_t)i * D.NP + mm] = shoup(x[m], __ldg(&D.tb.t4_f[i][mm]), p);
+        }
+    }
+    __syncthreads();
+}
+
 // src overrides the test's operand (x, or y for the second operand of a product)
 __global__ void __launch_bounds__(kColThreads) kn_col_fwd(const Desc *descs, const int2 *items, int nitems,
                                                           int second, const uint64_t *src_o) {
     extern __shared__ uint32_t sm[];
-    __shared__ StageConst K;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const int2 wi = items[it];
         const Desc &D = descs[wi.x];
-        const int R = (int)D.R, C = (int)D.C, g = wi.y;
         const uint64_t *src = src_o ? src_o : (second ? D.y : D.x);
         uint32_t *dst = second ? D.res2 : D.res;
-        load_const(&K, D, D.tb.twr_f);
-        for (int e = threadIdx.x; e < R * kG; e += blockDim.x) {
-            const int r = e / kG, l = e % kG;
-            const uint32_t j = (uint32_t)r * C + g * kG + l;
-            const uint64_t word = j < D.W ? src[j] : 0;
-#pragma unroll
-            for (int i = 0; i < kPrimes; i++) sm[(i * R + r) * kG + l] = residue(word, D.pr[i]);
+        switch (log2i(D.R)) {
+        case 3: col_fwd_item<2, 4>(sm, D, wi.y, src, dst); break;
+        case 4: col_fwd_item<4, 4>(sm, D, wi.y, src, dst); break;
+        case 5: col_fwd_item<4, 8>(sm, D, wi.y, src, dst); break;
+        case 6: col_fwd_item<8, 8>(sm, D, wi.y, src, dst); break;
+        case 7: col_fwd_item<8, 16>(sm, D, wi.y, src, dst); break;
+        case 8: col_fwd_item<16, 16>(sm, D, wi.y, src, dst); break;
+        case 9: col_fwd_item<16, 32>(sm, D, wi.y, src, dst); break;
+        default: col_fwd_item<32, 32>(sm, D, wi.y, src, dst); break;
         }
-        __syncthreads();
-        const int lR = log2i(R);
-        ntt_forward(sm, Shape{lR, 3, 3, lR + 3, kPrimes}, K);
-        for (int e = threadIdx.x; e < kPrimes * R * kG; e += blockDim.x) {
-            const int l = e % kG, t = e / kG, pos = t % R, i = t / R;
-            const uint32_t m = (uint32_t)pos * C + g * kG + l;
-            dst[(size_t)i * D.NP + m] = shoup(sm[(i * R + pos) * kG + l], __ldg(&D.tb.t4_f[i][m]), D.pr[i].p);
-        }
-        __syncthreads();
     }
 }
 
-// shared memory [operand][prime][c]
+// Row layout in shared memory: [operand][prime][padded c].
+template <int A, int B, bool MUL>
+__device__ __forceinline__ void row_item(uint32_t *sm, const Desc &D, int pos) {
+    constexpr int C = A * B, CP = C + C / B, lB = clog2<B>(), lA = clog2<A>();
+    constexpr int nops = MUL ? 2 : 1;
+    // wide forward levels straight from global memory
+    for (int u = threadIdx.x; u < nops * kPrimes * B; u += blockDim.x) {
+        const int t = u & (B - 1), i = (u >> lB) & (kPrimes - 1), op = u >> (lB + 2);
+        const uint32_t *src = op ? D.res2 : D.res;
+        const size_t base = (size_t)i * D.NP + (size_t)pos * C + t;
+        uint32_t x[A];
+#pragma unroll
+        for (int m = 0; m < A; m++) x[m] = src[base + B * m];
+        dif_regs<A>(x, t, B, D.tb.twc_f[i], D.pr[i].p);
+        uint32_t *row = sm + (op * kPrimes + i) * CP;
+#pragma unroll
+        for (int m = 0; m < A; m++) row[t + B * m + m] = x[m];
+    }
+    __syncthreads();
+    // narrow forward levels, the pointwise product, narrow inverse levels
+    for (int u = threadIdx.x; u < kPrimes * A; u += blockDim.x) {
+        const int t2 = u & (A - 1), i = u >> lA;
+        uint32_t *row = sm + i * CP + (B + 1) * t2;
+        const uint32_t p = D.pr[i].p, pinv = D.pr[i].pinv;
+        uint32_t x[B];
+#pragma unroll
+        for (int m = 0; m < B; m++) x[m] = row[m];
+        dif_regs<B>(x, B * t2, 1, D.tb.twc_f[i], p);
+        if (MUL) {
+            const uint32_t *rowy = sm + (kPrimes + i) * CP + (B + 1) * t2;
+            uint32_t y[B];
+#pragma unroll
+            for (int m = 0; m < B; m++) y[m] = rowy[m];
+            dif_regs<B>(y, B * t2, 1, D.tb.twc_f[i], p);
+#pragma unroll
+            for (int m = 0; m < B; m++) x[m] = montmul(x[m], y[m], p, pinv);
+        } else {
+#pragma unroll
+            for (int m = 0; m < B; m++) x[m] = montmul(x[m], x[m], p, pinv);
+        }
+        dit_regs<B>(x, B * t2, 1, D.tb.twc_i[i], p);
+#pragma unroll
+        for (int m = 0; m < B; m++) row[m] = x[m];
+    }
+    __syncthreads();
+    // wide inverse levels straight to global memory
+    for (int u = threadIdx.x; u < kPrimes * B; u += blockDim.x) {
+        const int t = u & (B - 1), i = u >> lB;
+        const uint32_t *row = sm + i * CP;
+        uint32_t x[A];
+#pragma unroll
+        for (int m = 0; m < A; m++) x[m] = row[t + B * m + m];
+        dit_regs<A>(x, t, B, D.tb.twc_i[i], D.pr[i].p);
+        const size_t base = (size_t)i * D.NP + (size_t)pos * C + t;
+#pragma unroll
+        for (int m = 0; m < A; m++) D.res[base + B * m] = x[m];
+    }
+    __syncthreads();
+}
+
 template <bool MUL>
 __global__ void __launch_bounds__(kRowThreads) kn_rows(const Desc *descs, const int2 *items, int nitems) {
     extern __shared__ uint32_t sm[];
-    __shared__ StageConst Kf, Ki;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const int2 wi = items[it];
         const Desc &D = descs[wi.x];
-        const int C = (int)D.C, pos = wi.y;
-        load_const(&Kf, D, D.tb.twc_f);
-        load_const(&Ki, D, D.tb.twc_i);
-        for (int e = threadIdx.x; e < kPrimes * C; e += blockDim.x) {
-            const size_t m = (size_t)(e / C) * D.NP + (size_t)pos * C + (e % C);
-            sm[e] = D.res[m];
-            if (MUL) sm[kPrimes * C + e] = D.res2[m];
+        switch (log2i(D.C)) {
+        case 3: row_item<2, 4, MUL>(sm, D, wi.y); break;
+        case 4: row_item<4, 4, MUL>(sm, D, wi.y); break;
+        case 5: row_item<4, 8, MUL>(sm, D, wi.y); break;
+        case 6: row_item<8, 8, MUL>(sm, D, wi.y); break;
+        case 7: row_item<8, 16, MUL>(sm, D, wi.y); break;
+        case 8: row_item<16, 16, MUL>(sm, D, wi.y); break;
+        case 9: row_item<16, 32, MUL>(sm, D, wi.y); break;
+        default: row_item<32, 32, MUL>(sm, D, wi.y); break;
         }
-        __syncthreads();
-        const int lC = log2i(C);
-        const Shape S{lC, 0, 0, lC, kPrimes};
-        ntt_forward(sm, S, Kf);
-        if (MUL) ntt_forward(sm + kPrimes * C, S, Kf);
-        for (int e = threadIdx.x; e < kPrimes * C; e += blockDim.x) {
-            const int i = e >> lC;
-            const uint32_t a = sm[e];
-            sm[e] = montmul(a, MUL ? sm[kPrimes * C + e] : a, D.pr[i].p, D.pr[i].pinv);
-        }
-        __syncthreads();
-        ntt_inverse(sm, S, Ki);
-        for (int e = threadIdx.x; e < kPrimes * C; e += blockDim.x)
-            D.res[(size_t)(e >> lC) * D.NP + (size_t)pos * C + (e & (C - 1))] = sm[e];
-        __syncthreads();
     }
 }
 
@@ -319,31 +318,84 @@ __device__ __forceinline__ ulonglong2 garner(const uint32_t *v, const Desc &D) {
     return make_ulonglong2((unsigned long long)c, (unsigned long long)(c >> 64));
 }
 
+template <int A, int B>
+__device__ __forceinline__ void col_inv_item(uint32_t *sm, const Desc &D, int g) {
+    constexpr int R = A * B, RP = R + R / B;
+    const int C = (int)D.C;
+    // narrow inverse levels straight from global memory, after the inverse four-step twiddle
+    for (int u = threadIdx.x; u < kPrimes * A * kG; u += blockDim.x) {
+        const int l = u & 7, t2 = (u >> 3) & (A - 1), i = u >> (3 + clog2<A>());
+        const uint32_t p = D.pr[i].p;
+        uint32_t x[B];
+#pragma unroll
+        for (int m = 0; m < B; m++) {
+            const uint32_t mm = (uint32_t)(B * t2 + m) * C + g * kG + l;
+            x[m] = shoup(D.res[(size_t)i * D.NP + mm], __ldg(&D.tb.t4_i[i][mm]), p);
+        }
+        dit_regs<B>(x, B * t2, 1, D.tb.twr_i[i], p);
+#pragma unroll
+        for (int m = 0; m < B; m++) sm[col_addr<B>(i, RP, B * t2 + m, l)] = x[m];
+    }
+    __syncthreads();
+    // wide inverse levels
+    for (int u = threadIdx.x; u < kPrimes * B * kG; u += blockDim.x) {
+        const int l = u & 7, t = (u >> 3) & (B - 1), i = u >> (3 + clog2<B>());
+        uint32_t x[A];
+#pragma unroll
+        for (int m = 0; m < A; m++) x[m] = sm[col_addr<B>(i, RP, t + B * m, l)];
+        dit_regs<A>(x, t, B, D.tb.twr_i[i], D.pr[i].p);
+#pragma unroll
+        for (int m = 0; m < A; m++) sm[col_addr<B>(i, RP, t + B * m, l)] = x[m];
+    }
+    __syncthreads();
+    // Row r of the group holds the coefficients r C + 8 g .. + 7, one per lane of an 8-lane group
+    // of a warp: the CRT per lane, then the carry through the 8 lanes by shuffles (7 rounds
+    // settle any chain), giving 8 words of P and the segment's carry-out.
+    const uint32_t w = D.w;
+    const uint64_t M = (1ull << w) - 1;
+    for (int e = threadIdx.x; e < R * kG; e += blockDim.x) {  // whole warps: R * kG is a multiple of 32
+        const int r = e >> 3, l = e & 7;
+        uint32_t v[kPrimes];
+#pragma unroll
+        for (int i = 0; i < kPrimes; i++) v[i] = red2(sm[col_addr<B>(i, RP, r, l)], D.pr[i].p);
+        const ulonglong2 c2 = garner(v, D);
+        const u128 c = ((u128)c2.y << 64) | c2.x;
+        u128 a = c;
+#pragma unroll
+        for (int round = 0; round < kG - 1; round++) {
+            const u128 cy = a >> w;
+            const uint32_t q0 = __shfl_up_sync(0xffffffffu, (uint32_t)cy, 1, kG);
+            const uint32_t q1 = __shfl_up_sync(0xffffffffu, (uint32_t)(cy >> 32), 1, kG);
+            const uint32_t q2 = __shfl_up_sync(0xffffffffu, (uint32_t)(cy >> 64), 1, kG);
+            const uint32_t q3 = __shfl_up_sync(0xffffffffu, (uint32_t)(cy >> 96), 1, kG);
+            const u128 cin = l ? (((u128)q3 << 96) | ((u128)q2 << 64) | ((u128)q1 << 32) | q0) : 0;
+            a = c + cin;
+        }
+        const uint32_t j = (uint32_t)r * C + g * kG + l;
+        D.pw[j] = (uint64_t)a & M;
+        if (l == kG - 1) {
+            const u128 out = a >> w;
+            D.seg[j >> 3] = make_ulonglong2((unsigned long long)out, (unsigned long long)(out >> 64));
+        }
+    }
+    __syncthreads();
+}
+
 __global__ void __launch_bounds__(kColThreads) kn_col_inv(const Desc *descs, const int2 *items, int nitems) {
     extern __shared__ uint32_t sm[];
-    __shared__ StageConst K;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
         const int2 wi = items[it];
         const Desc &D = descs[wi.x];
-        const int R = (int)D.R, C = (int)D.C, g = wi.y;
-        load_const(&K, D, D.tb.twr_i);
-        for (int e = threadIdx.x; e < kPrimes * R * kG; e += blockDim.x) {
-            const int l = e % kG, t = e / kG, pos = t % R, i = t / R;
-            const uint32_t m = (uint32_t)pos * C + g * kG + l;
-            sm[(i * R + pos) * kG + l] = shoup(D.res[(size_t)i * D.NP + m], __ldg(&D.tb.t4_i[i][m]), D.pr[i].p);
+        switch (log2i(D.R)) {
+        case 3: col_inv_item<2, 4>(sm, D, wi.y); break;
+        case 4: col_inv_item<4, 4>(sm, D, wi.y); break;
+        case 5: col_inv_item<4, 8>(sm, D, wi.y); break;
+        case 6: col_inv_item<8, 8>(sm, D, wi.y); break;
+        case 7: col_inv_item<8, 16>(sm, D, wi.y); break;
+        case 8: col_inv_item<16, 16>(sm, D, wi.y); break;
+        case 9: col_inv_item<16, 32>(sm, D, wi.y); break;
+        default: col_inv_item<32, 32>(sm, D, wi.y); break;
         }
-        __syncthreads();
-        const int lR = log2i(R);
-        ntt_inverse(sm, Shape{lR, 3, 3, lR + 3, kPrimes}, K);
-        for (int e = threadIdx.x; e < R * kG; e += blockDim.x) {
-            const int r = e / kG, l = e % kG;
-            const uint32_t j = (uint32_t)r * C + g * kG + l;
-            uint32_t v[kPrimes];
-#pragma unroll
-            for (int i = 0; i < kPrimes; i++) v[i] = red2(sm[(i * R + r) * kG + l], D.pr[i].p);
-            D.coef[j] = j < D.NU ? garner(v, D) : make_ulonglong2(0, 0);
-        }
-        __syncthreads();
     }
 }
 
@@ -385,70 +437,107 @@ __global__ void __launch_bounds__(kReduceThreads) kn_reduce(const Desc *descs, c
     const int t = threadIdx.x, T = blockDim.x;
     const uint32_t w = D.w;
     const uint64_t M = (1ull << w) - 1;
-    // 1. product words: P = sum coef_j 2^(w j)
+    // The descriptor's fields are read once: the stores below go through global pointers the
+    // compiler cannot tell apart from the descriptor.
+    const uint32_t NP = D.NP, Wn = D.W, WN0 = D.WN0, BN0 = D.BN0;
+    const uint64_t kk = D.k;
+    const ulonglong2 *__restrict__ seg = D.seg;
+    uint64_t *__restrict__ pw = D.pw;
+    int *status = D.status;
+    constexpr int U = 8;  // loads in flight per thread
+    // 1. product words: the transform kernels left P as 8-word segments, each normalised, with
+    //    the carry out of segment s in seg[s]; add every segment's carry into the next one
     {
-        const uint32_t S = (D.NU + T - 1) / T;
+        const uint32_t nseg = NP >> 3, per = (nseg + T - 1) / T;
+        const uint32_t s0 = (uint32_t)t * per, s1 = min(nseg, s0 + per);
         u128 acc = 0;
-        const uint32_t j0 = (uint32_t)t * S, e = min(D.NU, j0 + S);
-        for (uint32_t j = j0; j < e; j++) {
-            const ulonglong2 c = D.coef[j];
+        for (uint32_t sg = s0; sg < s1; sg++) {
+            if (sg > s0) {
+                const ulonglong2 c = seg[sg - 1];
+                acc += ((u128)c.y << 64) | c.x;
+            }
+            for (uint32_t j = sg << 3; acc != 0 && j < (sg << 3) + 8; j++) {
+                acc += pw[j];
+                pw[j] = (uint64_t)acc & M;
+                acc >>= w;
+            }
+        }
+        if (s1 > s0) {
+            const ulonglong2 c = seg[s1 - 1];
             acc += ((u128)c.y << 64) | c.x;
-            D.pw[j] = (uint64_t)acc & M;
-            acc >>= w;
         }
         co[t] = acc;
-        if (resolve_chunks(D.pw, D.NU, S, w, co, &top) != 0 && t == 0) atomicOr(D.status, 1);
+        if (resolve_chunks(pw, NP, per << 3, w, co, &top) != 0 && t == 0) atomicOr(status, 1);
     }
     // 2. Montgomery reduction E = B + k A (+ addend), P = A + B 2^n
     {
-        const uint32_t S = (D.W + T - 1) / T;
-        const uint32_t WN0 = D.WN0, BN0 = D.BN0, NU = D.NU;
+        const uint32_t S = (Wn + T - 1) / T;
         const uint64_t lowmask = (1ull << BN0) - 1;
         u128 acc = 0;
-        const uint32_t j0 = (uint32_t)t * S, e = min(D.W, j0 + S);
-        for (uint32_t j = j0; j < e; j++) {
-            const uint64_t a = j < WN0 ? D.pw[j] : (j == WN0 ? (D.pw[j] & lowmask) : 0);
-            const uint32_t s = WN0 + j;
-            const uint64_t lo = s < NU ? D.pw[s] : 0, hi = s + 1 < NU ? D.pw[s + 1] : 0;
-            const uint64_t b = BN0 ? (((lo >> BN0) | (hi << (w - BN0))) & M) : lo;
-            acc += (u128)b + (u128)D.k * a + (addend ? addend[j] : 0);
-            X[j] = (uint64_t)acc & M;
-            acc >>= w;
+        const uint32_t j0 = (uint32_t)t * S, e = min(Wn, j0 + S);
+        for (uint32_t j = j0; j < e; j += U) {
+            uint64_t a[U], bw[U + 1], ad[U];
+#pragma unroll
+            for (int q = 0; q < U; q++) {
+                const uint32_t jj = j + q;
+                a[q] = jj < WN0 ? pw[jj] : (jj == WN0 ? (pw[jj] & lowmask) : 0);
+                ad[q] = addend && jj < e ? addend[jj] : 0;
+            }
+#pragma unroll
+            for (int q = 0; q <= U; q++) {
+                const uint32_t s2 = WN0 + j + q;
+                bw[q] = s2 < NP ? pw[s2] : 0;
+            }
+#pragma unroll
+            for (int q = 0; q < U; q++) {
+                if (j + q >= e) break;
+                const uint64_t b = BN0 ? (((bw[q] >> BN0) | (bw[q + 1] << (w - BN0))) & M) : bw[q];
+                acc += (u128)b + (u128)kk * a[q] + ad[q];
+                X[j + q] = (uint64_t)acc & M;
+                acc >>= w;
+            }
         }
         co[t] = acc;
-        if (resolve_chunks(X, D.W, S, w, co, &top) != 0 && t == 0) atomicOr(D.status, 2);
+        if (resolve_chunks(X, Wn, S, w, co, &top) != 0 && t == 0) atomicOr(status, 2);
     }
     // 3. top fold: T = x >> n = q k + r; x <- x mod 2^n + q + r 2^n
     if (t == 0) {
         uint64_t *x = X;
-        const uint32_t WN0 = D.WN0, BN0 = D.BN0;
         u128 Tv = x[WN0] >> BN0;
         uint32_t sh = w - BN0;
-        for (uint32_t j = WN0 + 1; j < D.W; j++) {
+        for (uint32_t j = WN0 + 1; j < Wn; j++) {
             if (x[j]) {
-                if (sh >= 128 || (sh > 64 && (x[j] >> (128 - sh)) != 0)) atomicOr(D.status, 4);
+                if (sh >= 128 || (sh > 64 && (x[j] >> (128 - sh)) != 0)) atomicOr(status, 4);
                 else Tv |= (u128)x[j] << sh;
             }
             sh += w;
             x[j] = 0;
         }
         x[WN0] &= (1ull << BN0) - 1;
-        const u128 q = Tv / D.k;
-        const uint64_t r = (uint64_t)(Tv - q * D.k);
+        u128 q;
+        uint64_t r;
+        if ((uint64_t)(Tv >> 64) == 0) {  // always for k < 2^30: T < 2^(2 log2 k + 3)
+            const uint64_t t64 = (uint64_t)Tv;
+            q = t64 / kk;
+            r = t64 - (uint64_t)q * kk;
+        } else {
+            q = Tv / kk;
+            r = (uint64_t)(Tv - q * kk);
+        }
         u128 add = (u128)r << BN0;
-        for (uint32_t j = WN0; add != 0 && j < D.W; j++) {
+        for (uint32_t j = WN0; add != 0 && j < Wn; j++) {
             add += x[j];
             x[j] = (uint64_t)add & M;
             add >>= w;
         }
-        if (add) atomicOr(D.status, 8);
+        if (add) atomicOr(status, 8);
         add = q;
-        for (uint32_t j = 0; add != 0 && j < D.W; j++) {
+        for (uint32_t j = 0; add != 0 && j < Wn; j++) {
             add += x[j];
             x[j] = (uint64_t)add & M;
             add >>= w;
         }
-        if (add) atomicOr(D.status, 8);
+        if (add) atomicOr(status, 8);
     }
 }
 
@@ -496,6 +585,15 @@ int ilog2(uint32_t x) {
     while ((1u << b) < x) b++;
     return b;
 }
+
+// shared memory of the transform kernels for a length-n transform split A x B (B = 2^ceil(log2 n / 2)),
+// stored padded: n + n / B elements
+size_t padded_len(uint32_t n) {
+    const int l = ilog2(n);
+    return (size_t)n + (n >> ((l + 1) / 2));
+}
+size_t col_smem_bytes(uint32_t R) { return (size_t)kPrimes * padded_len(R) * kG * 4; }
+size_t row_smem_bytes(uint32_t C) { return (size_t)kPrimes * padded_len(C) * 4; }
 
 struct Plan {
     uint32_t NP = 0, R = 0, C = 0;
@@ -626,7 +724,7 @@ struct kn_engine {
     int *d_test = nullptr;
     int *d_status = nullptr;
     uint32_t *d_res = nullptr, *d_res2 = nullptr;
-    ulonglong2 *d_coef = nullptr;
+    ulonglong2 *d_seg = nullptr;
     uint64_t *d_pw = nullptr;
     uint64_t *d_addend = nullptr;
     int64_t addend_c = 0;
@@ -833,7 +931,7 @@ kn_engine *kn_engine_new(uint64_t k, uint64_t n, int device) {
               kok(e, cudaMalloc((void **)&e->d_desc, sizeof(Desc))) &&
               kok(e, cudaMalloc((void **)&e->d_res, (size_t)kPrimes * NP * 4)) &&
               kok(e, cudaMalloc((void **)&e->d_res2, (size_t)kPrimes * NP * 4)) &&
-              kok(e, cudaMalloc((void **)&e->d_coef, (size_t)NP * sizeof(ulonglong2))) &&
+              kok(e, cudaMalloc((void **)&e->d_seg, (size_t)(NP / kG) * sizeof(ulonglong2))) &&
               kok(e, cudaMalloc((void **)&e->d_pw, (size_t)NP * 8)) &&
               kok(e, cudaMalloc((void **)&e->d_addend, (size_t)e->W * 8)) &&
               kok(e, cudaMalloc((void **)&e->d_status, sizeof(int))) &&
@@ -850,7 +948,7 @@ kn_engine *kn_engine_new(uint64_t k, uint64_t n, int device) {
              kok(e, cudaMemcpy(e->d_test, &zero, sizeof zero, cudaMemcpyHostToDevice)) &&
              kok(e, cudaMemcpy(e->d_status, &zero, sizeof zero, cudaMemcpyHostToDevice));
     }
-    if (ok) ok = prepare_smem(device, (size_t)kPrimes * R * kG * 4, (size_t)2 * kPrimes * C * 4);
+    if (ok) ok = prepare_smem(device, col_smem_bytes(R), 2 * row_smem_bytes(C));
     if (!ok) {
         kn_engine_free(e);
         return nullptr;
@@ -860,14 +958,13 @@ kn_engine *kn_engine_new(uint64_t k, uint64_t n, int device) {
     d.R = R;
     d.C = C;
     d.W = e->W;
-    d.NU = std::min<uint32_t>(NP, 2 * e->W);
     d.w = e->w;
     d.WN0 = (uint32_t)(n / e->w);
     d.BN0 = (uint32_t)(n % e->w);
     d.k = k;
     d.res = e->d_res;
     d.res2 = e->d_res2;
-    d.coef = e->d_coef;
+    d.seg = e->d_seg;
     d.pw = e->d_pw;
     d.status = e->d_status;
     d.tb = e->plan->tb;
@@ -898,7 +995,7 @@ void kn_engine_free(kn_engine *e) {
     if (!e) return;
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
-    for (void *p : {(void *)e->d_desc, (void *)e->d_res, (void *)e->d_res2, (void *)e->d_coef, (void *)e->d_pw,
+    for (void *p : {(void *)e->d_desc, (void *)e->d_res, (void *)e->d_res2, (void *)e->d_seg, (void *)e->d_pw,
                     (void *)e->d_addend, (void *)e->d_status, (void *)e->d_cols, (void *)e->d_rows, (void *)e->d_test})
         if (p) cudaFree(p);
     if (e->stream) cudaStreamDestroy(e->stream);
@@ -971,7 +1068,7 @@ int kn_get_limbs(kn_engine *e, const uint64_t *x, uint64_t *limbs) {
 
 static int run_product(kn_engine *e, uint64_t *x, const uint64_t *y, const uint64_t *addend) {
     const uint32_t R = e->plan->R, C = e->plan->C;
-    const size_t col_smem = (size_t)kPrimes * R * kG * 4, row_smem = (size_t)kPrimes * C * 4;
+    const size_t col_smem = col_smem_bytes(R), row_smem = row_smem_bytes(C);
     const int ncols = (int)(C / kG), nrows = (int)R;
     kn_col_fwd<<<ncols, kColThreads, col_smem, e->stream>>>(e->d_desc, e->d_cols, ncols, 0, x);
     if (y) {
@@ -1092,8 +1189,8 @@ bool group_build(kn_group *g) {
         tests[t] = t;
         for (uint32_t c = 0; c < e->plan->C / kG; c++) cols.push_back(make_int2(t, (int)c));
         for (uint32_t r = 0; r < e->plan->R; r++) rows.push_back(make_int2(t, (int)r));
-        g->col_smem = std::max(g->col_smem, (size_t)kPrimes * e->plan->R * kG * 4);
-        g->row_smem = std::max(g->row_smem, (size_t)kPrimes * e->plan->C * 4);
+        g->col_smem = std::max(g->col_smem, col_smem_bytes(e->plan->R));
+        g->row_smem = std::max(g->row_smem, row_smem_bytes(e->plan->C));
     }
     g->ncols = (int)cols.size();
     g->nrows = (int)rows.size();
