@@ -349,8 +349,10 @@ __device__ __forceinline__ void col_inv_item(uint32_t *sm, const Desc &D, int g)
     }
     __syncthreads();
     // Row r of the group holds the coefficients r C + 8 g .. + 7, one per lane of an 8-lane group
-    // of a warp: the CRT per lane, then the carry through the 8 lanes by shuffles (7 rounds
-    // settle any chain), giving 8 words of P and the segment's carry-out.
+    // of a warp.  Each lane splits its coefficient c_l < W 2^2w into w-bit parts lo + mid 2^w +
+    // hi 2^2w (hi < W <= 2^20); word l of the segment collects s_l = lo_l + mid_(l-1) + hi_(l-2)
+    // < 2^(w+2), so the carries between lanes are at most 3 and settle in 7 shuffle rounds.
+    // Lane 7 also keeps what leaves the segment: mid_7 + hi_6 + hi_7 2^w plus its carry.
     const uint32_t w = D.w;
     const uint64_t M = (1ull << w) - 1;
     for (int e = threadIdx.x; e < R * kG; e += blockDim.x) {  // whole warps: R * kG is a multiple of 32
@@ -360,21 +362,26 @@ __device__ __forceinline__ void col_inv_item(uint32_t *sm, const Desc &D, int g)
         for (int i = 0; i < kPrimes; i++) v[i] = red2(sm[col_addr<B>(i, RP, r, l)], D.pr[i].p);
         const ulonglong2 c2 = garner(v, D);
         const u128 c = ((u128)c2.y << 64) | c2.x;
-        u128 a = c;
+        const uint64_t lo = (uint64_t)c & M, mid = (uint64_t)(c >> w) & M;
+        const uint32_t hi = (uint32_t)(c >> (2 * w));
+        const uint32_t mid_lo = __shfl_up_sync(0xffffffffu, (uint32_t)mid, 1, kG);
+        const uint32_t mid_hi = __shfl_up_sync(0xffffffffu, (uint32_t)(mid >> 32), 1, kG);
+        const uint32_t hi1 = __shfl_up_sync(0xffffffffu, hi, 1, kG);
+        const uint32_t hi2 = __shfl_up_sync(0xffffffffu, hi, 2, kG);
+        const uint64_t sl = lo + (l >= 1 ? ((uint64_t)mid_hi << 32 | mid_lo) : 0) + (l >= 2 ? hi2 : 0);
+        const uint64_t rl = sl & M;
+        const uint32_t gl = (uint32_t)(sl >> w);
+        uint32_t cout = gl;
 #pragma unroll
         for (int round = 0; round < kG - 1; round++) {
-            const u128 cy = a >> w;
-            const uint32_t q0 = __shfl_up_sync(0xffffffffu, (uint32_t)cy, 1, kG);
-            const uint32_t q1 = __shfl_up_sync(0xffffffffu, (uint32_t)(cy >> 32), 1, kG);
-            const uint32_t q2 = __shfl_up_sync(0xffffffffu, (uint32_t)(cy >> 64), 1, kG);
-            const uint32_t q3 = __shfl_up_sync(0xffffffffu, (uint32_t)(cy >> 96), 1, kG);
-            const u128 cin = l ? (((u128)q3 << 96) | ((u128)q2 << 64) | ((u128)q1 << 32) | q0) : 0;
-            a = c + cin;
+            const uint32_t cin = __shfl_up_sync(0xffffffffu, cout, 1, kG);
+            cout = gl + (uint32_t)((rl + (l ? cin : 0)) >> w);
         }
+        const uint32_t cin = __shfl_up_sync(0xffffffffu, cout, 1, kG);
         const uint32_t j = (uint32_t)r * C + g * kG + l;
-        D.pw[j] = (uint64_t)a & M;
+        D.pw[j] = (rl + (l ? cin : 0)) & M;
         if (l == kG - 1) {
-            const u128 out = a >> w;
+            const u128 out = (u128)mid + hi1 + cout + ((u128)hi << w);
             D.seg[j >> 3] = make_ulonglong2((unsigned long long)out, (unsigned long long)(out >> 64));
         }
     }
@@ -1211,7 +1218,8 @@ bool group_build(kn_group *g) {
 void group_square_once(kn_group *g) {
     const int gc = std::min(g->ncols, g->grid), gr = std::min(g->nrows, g->grid);
     kn_col_fwd<<<gc, g->threads, g->col_smem, g->stream>>>(g->d_desc, g->d_cols, g->ncols, 0, nullptr);
-    kn_rows<false><<<gr, g->threads, g->row_smem, g->stream>>>(g->d_desc, g->d_rows, g->nrows);
+    // a row item is 4 B units per register pass (B = 16 for the common C = 256): 64 threads
+    kn_rows<false><<<std::min(g->nrows, 2 * g->grid), 64, g->row_smem, g->stream>>>(g->d_desc, g->d_rows, g->nrows);
     kn_col_inv<<<gc, g->threads, g->col_smem, g->stream>>>(g->d_desc, g->d_cols, g->ncols);
     kn_reduce<<<g->ntests, kReduceThreads, 0, g->stream>>>(g->d_desc, g->d_tests, nullptr, nullptr);
 }
