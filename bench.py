@@ -353,46 +353,15 @@ def ntt_leg(lib, tests, mean_n, device, squarings=64, reps=3):
     test's number squared `squarings` times per timed call (CUDA events on the group's stream).
     tests/hour counts a Gerbicz block as B squarings plus one product, a product as two
     squarings, and the check every M blocks, as the FP64 line does."""
-    import ctypes as C
-    engines, xs = [], []
-    g = lib.kn_group_new(device)
-    try:
-        for k, n in tests:
-            e = lib.kn_engine_new(k, n, device)
-            if not e:
-                raise RuntimeError(f"kn_engine_new({k}, {n}) failed")
-            engines.append(e)
-            x = lib.kn_num_alloc(e)
-            xs.append(x)
-            limbs = (C.c_uint64 * lib.kn_limbs(e))()
-            limbs[0] = 3
-            lib.kn_set_limbs(e, x, limbs)
-            lib.kn_group_add(g, e, x)
-        nps = {}
-        for e in engines:
-            L = lib.kn_transform_len(e)
-            nps[L] = nps.get(L, 0) + 1
-        ms = C.c_float(0)
-        if lib.kn_group_square(g, 16, C.byref(ms)) != 0:
-            raise RuntimeError("kn_group_square failed")
-        times = []
-        for _ in range(reps):
-            if lib.kn_group_square(g, squarings, C.byref(ms)) != 0:
-                raise RuntimeError("kn_group_square failed")
-            times.append(ms.value * 1e-3 / squarings)
-        t_sq = statistics.median(times)
-        t_block = (BLOCK + 2) * t_sq
-        tph = 3600.0 * len(tests) * BLOCK / (t_block * (1 + 1 / BLOCKS_PER_CHECK) * mean_n)
-        return {"tests_per_hour": tph, "ms_per_squaring_step": t_sq * 1e3,
-                "us_per_test_squaring": t_sq * 1e6 / len(tests),
-                "transform_lengths": {str(k): v for k, v in sorted(nps.items())},
-                "gpu_launches_per_squaring": 4,
-                "arithmetic": "exact: residues mod four 30-bit primes, Garner CRT, Montgomery R=2^n"}
-    finally:
-        lib.kn_group_free(g)
-        for e, x in zip(engines, xs):
-            lib.kn_num_free(e, x)
-            lib.kn_engine_free(e)
+    from ahnum_gb300.ntt_group import time_steps
+    t_sq, nps = time_steps(tests, squarings, reps, device)
+    t_block = (BLOCK + 2) * t_sq
+    tph = 3600.0 * len(tests) * BLOCK / (t_block * (1 + 1 / BLOCKS_PER_CHECK) * mean_n)
+    return {"tests_per_hour": tph, "ms_per_squaring_step": t_sq * 1e3,
+            "us_per_test_squaring": t_sq * 1e6 / len(tests),
+            "transform_lengths": {str(k): v for k, v in nps.items()},
+            "gpu_launches_per_squaring": 4,
+            "arithmetic": "exact: residues mod four 30-bit primes, Garner CRT, Montgomery R=2^n"}
 
 
 _len_cache = {}
