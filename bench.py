@@ -309,6 +309,8 @@ def run_ours(args):
         c.sync()
         us_sq_49152 = (time.perf_counter() - s0) / 1000 * 1e6
 
+    large = large_segment(lib) if rank == 0 else None
+
     cpu = None
     if rank == 0:
         threads = os.cpu_count() or 1
@@ -341,11 +343,51 @@ def run_ours(args):
                             "us_per_squaring_by_L": {str(L): v * 1e6 for L, v in sorted(single.items())},
                             "batched_over_single": value / world / single_tph},
             "cpu_baseline": cpu,
+            "large_single_test": large,
             "ntt_engine": ntt,
         }
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def large_segment(lib, seed=4, squarings=100_000, block=1000, blocks_per_check=50):
+    """The large single test: a Fermat test of k*2^n-1, k odd seeded in [3, 255], n seeded in
+    [2e7, 2.5e7] (FFT length about 1.2-1.8 M words), stopped after `squarings` verified
+    squarings.  Gerbicz blocks of 1000 with a check every 50 blocks, so the segment holds two
+    checks.  Time per squaring from the progress callbacks (one per block, after a device sync),
+    checks included."""
+    import ctypes as C
+    import numpy as np
+    from ahnum_gb300 import native
+    rng = np.random.Generator(np.random.PCG64(seed))
+    k = int(rng.integers(1, 128)) * 2 + 1
+    n = int(rng.integers(20_000_000, 25_000_001))
+    flag = C.c_int(0)
+    marks = []
+
+    def progress(arg, it, nn, e):
+        marks.append((time.perf_counter(), int(it), float(e)))
+        if it >= squarings:
+            flag.value = 1
+
+    cb = native.PROGRESS_FN(progress)
+    o = native.KitePrpOpts()
+    o.fft = native.KiteOpts(native.KITE_BACKEND_CUDA, 0, 0, 0)
+    o.gerbicz_block = block
+    o.gerbicz_blocks = blocks_per_check
+    o.progress = cb
+    o.abort_flag = C.pointer(flag)
+    r = native.KitePrpResult()
+    t0 = time.perf_counter()
+    rc = lib.kite_prp(k, n, 3, C.byref(o), C.byref(r))
+    wall = time.perf_counter() - t0
+    (ta, ia, _), (tb, ib, _) = marks[0], marks[-1]
+    return {"k": k, "n": n, "fft_len": lib.kc_choose_fft_len(k, n), "squarings": ib,
+            "us_per_squaring": (tb - ta) / (ib - ia) * 1e6, "wall_s": wall,
+            "gerbicz_block": block, "gerbicz_blocks_per_check": blocks_per_check,
+            "gerbicz_errors": r.gerbicz_errors, "maxerr": max(e for _, _, e in marks),
+            "stopped_on_request": rc == -5}
 
 
 def ntt_leg(lib, tests, mean_n, device, squarings=64, reps=3):
