@@ -1144,6 +1144,8 @@ struct kn_group {
     cudaStream_t stream = nullptr;
     std::vector<kn_engine *> eng;
     std::vector<uint64_t *> xs;
+    std::vector<Desc> h_desc;  // the device table's host copy, in work-list order
+    std::vector<int> slot;     // member -> its index in the table
     Desc *d_desc = nullptr;
     int2 *d_cols = nullptr, *d_rows = nullptr;
     int *d_tests = nullptr;
@@ -1202,6 +1204,9 @@ bool group_build(kn_group *g) {
     g->ncols = (int)cols.size();
     g->nrows = (int)rows.size();
     g->ntests = m;
+    g->h_desc = descs;
+    g->slot.assign(m, 0);
+    for (int t = 0; t < m; t++) g->slot[order[t]] = t;
     bool ok = gok(g, cudaMalloc((void **)&g->d_desc, m * sizeof(Desc))) &&
               gok(g, cudaMalloc((void **)&g->d_cols, cols.size() * sizeof(int2))) &&
               gok(g, cudaMalloc((void **)&g->d_rows, rows.size() * sizeof(int2))) &&
@@ -1299,6 +1304,28 @@ int kn_group_square(kn_group *g, uint64_t count, float *gpu_ms) {
         if (st) g->err = -100 - st;
     }
     return g->err ? -1 : 0;
+}
+
+int kn_group_mul(kn_group *g, const uint64_t *const *ys, float *gpu_ms) {
+    if (!g || g->err || !ys) return -1;
+    if (g->eng.empty()) return 0;
+    cudaSetDevice(g->device);
+    if (!group_build(g)) return -1;
+    for (size_t i = 0; i < g->eng.size(); i++) g->h_desc[g->slot[i]].y = ys[i];
+    if (!gok(g, cudaMemcpyAsync(g->d_desc, g->h_desc.data(), g->h_desc.size() * sizeof(Desc),
+                                cudaMemcpyHostToDevice, g->stream)))
+        return -1;
+    const int gc = std::min(g->ncols, g->grid), gr = std::min(g->nrows, 2 * g->grid);
+    gok(g, cudaEventRecord(g->ev0, g->stream));
+    kn_col_fwd<<<gc, g->threads, g->col_smem, g->stream>>>(g->d_desc, g->d_cols, g->ncols, 0, nullptr);
+    kn_col_fwd<<<gc, g->threads, g->col_smem, g->stream>>>(g->d_desc, g->d_cols, g->ncols, 1, nullptr);
+    kn_rows<true><<<gr, 64, 2 * g->row_smem, g->stream>>>(g->d_desc, g->d_rows, g->nrows);
+    kn_col_inv<<<gc, g->threads, g->col_smem, g->stream>>>(g->d_desc, g->d_cols, g->ncols);
+    kn_reduce<<<g->ntests, kReduceThreads, 0, g->stream>>>(g->d_desc, g->d_tests, nullptr, nullptr);
+    gok(g, cudaEventRecord(g->ev1, g->stream));
+    if (!gok(g, cudaGetLastError()) || !gok(g, cudaStreamSynchronize(g->stream))) return -1;
+    if (gpu_ms) cudaEventElapsedTime(gpu_ms, g->ev0, g->ev1);
+    return 0;
 }
 
 int kn_group_error(const kn_group *g) { return g ? g->err : -1; }

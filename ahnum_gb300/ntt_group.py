@@ -74,6 +74,157 @@ class NttGroup:
         self.close()
 
 
+class NttFermatBatch:
+    """Fermat base-a PRP tests of many N = k*2^n-1 on the integer-NTT engine, in lockstep Gerbicz
+    blocks: every block squares all tests' x B times (one group launch set per squaring) and
+    multiplies d <- d*x (one group product); every M blocks, t = d before the block's product is
+    checked as x0 * t^(2^B) == d, the reference's check (src/prp.c:407-567), and the verified
+    (x, d) kept on the host; a failed check returns every test to its verified state.  A test
+    whose remaining squarings fall below a block leaves the group and finishes alone with a
+    doubled tail (the tail squared twice and compared), as kite_prp does."""
+
+    def __init__(self, tests, base: int = 3, block: int = 1000, blocks_per_check: int = 250,
+                 device: int = 0):
+        self.lib = native.load()
+        self.base, self.B, self.M, self.device = base, block, blocks_per_check, device
+        self.t = []
+        for k, n in tests:
+            e = self.lib.kn_engine_new(k, n, device)
+            if not e:
+                self.close()
+                raise RuntimeError(f"kn_engine_new({k}, {n}) failed")
+            N = k * (1 << n) - 1
+            st = {"k": k, "n": n, "N": N, "e": e, "nl": self.lib.kn_limbs(e), "done": 0,
+                  "res64": None, "is_prp": None, "gerbicz_errors": 0}
+            for name in ("x", "d", "t", "x0"):
+                st[name] = self.lib.kn_num_alloc(e)
+            x0 = pow(base, k, N)
+            for name in ("x", "d", "x0"):
+                self._set(st, name, x0)
+            st["vx"] = st["vd"] = x0
+            self.t.append(st)
+        self.gpu_ms = 0.0        # GPU time of every group operation
+        self.block_ms = 0.0      # of the blocks alone (B squarings and the product), checks excluded
+        self.blocks = 0
+        self.fault = None        # (k, squarings done): corrupt that test's x once, for tests
+
+    def _set(self, st, name, v):
+        arr = (C.c_uint64 * st["nl"])()
+        C.memmove(arr, v.to_bytes(8 * st["nl"], "little"), 8 * st["nl"])
+        if self.lib.kn_set_limbs(st["e"], st[name], arr) != 0:
+            raise RuntimeError("kn_set_limbs failed")
+
+    def _get(self, st, name) -> int:
+        arr = (C.c_uint64 * st["nl"])()
+        if self.lib.kn_get_limbs(st["e"], st[name], arr) != 0:
+            raise RuntimeError("kn_get_limbs failed")
+        return int.from_bytes(C.string_at(arr, 8 * st["nl"]), "little")
+
+    def _group(self, members, which):
+        g = self.lib.kn_group_new(self.device)
+        for st in members:
+            if self.lib.kn_group_add(g, st["e"], st[which]) < 0:
+                raise RuntimeError("kn_group_add failed")
+        return g
+
+    def _timed(self, rc, ms):
+        if rc != 0:
+            raise RuntimeError("kn_group operation failed")
+        self.gpu_ms += ms.value
+
+    def _square(self, g, count):
+        ms = C.c_float(0)
+        self._timed(self.lib.kn_group_square(g, count, C.byref(ms)), ms)
+
+    def _mul(self, g, members, which):
+        ys = (C.c_void_p * len(members))(*[st[which] for st in members])
+        ms = C.c_float(0)
+        self._timed(self.lib.kn_group_mul(g, ys, C.byref(ms)), ms)
+
+    def _finish(self, st):
+        """the last squarings (fewer than a block) twice, compared; then the residue"""
+        rest = st["n"] - st["done"]
+        e = st["e"]
+        self.lib.kn_copy(e, st["t"], st["x"])
+        self.lib.kn_square(e, st["x"], rest)
+        self.lib.kn_square(e, st["t"], rest)
+        a, b = self._get(st, "x"), self._get(st, "t")
+        if a != b:
+            raise RuntimeError("tail mismatch")
+        N = st["N"]
+        r = a * pow(self.base * self.base, -1, N) % N  # base^(N+1) -> base^(N-1)
+        st["res64"] = r & (2**64 - 1)
+        st["is_prp"] = r == 1
+        st["done"] = st["n"]
+
+    def run(self, max_blocks: int | None = None):
+        """Runs the tests to their residues (or `max_blocks` blocks); returns the results."""
+        blocks = 0
+        while True:
+            active = [st for st in self.t if st["res64"] is None and st["n"] - st["done"] >= self.B]
+            for st in self.t:
+                if st["res64"] is None and st not in active:
+                    self._finish(st)
+            if not active or (max_blocks is not None and blocks >= max_blocks):
+                break
+            gx, gd, gt = (self._group(active, w) for w in ("x", "d", "t"))
+            try:
+                # blocks until the next check, or until a test would leave the lockstep
+                room = min((st["n"] - st["done"]) // self.B for st in active)
+                span = min(self.M, room)
+                if max_blocks is not None:
+                    span = min(span, max_blocks - blocks)
+                for j in range(span):
+                    if j == span - 1:
+                        for st in active:
+                            self.lib.kn_copy(st["e"], st["t"], st["d"])
+                    before = self.gpu_ms
+                    self._square(gx, self.B)
+                    for st in active:
+                        st["done"] += self.B
+                        if self.fault and self.fault[0] == st["k"] and st["done"] == self.fault[1]:
+                            self._corrupt(st)
+                            self.fault = None
+                    self._mul(gd, active, "x")
+                    self.block_ms += self.gpu_ms - before
+                    self.blocks += 1
+                blocks += span
+                # check: x0 * t^(2^B) == d
+                self._square(gt, self.B)
+                self._mul(gt, active, "x0")
+                for st in active:
+                    if self._get(st, "t") == self._get(st, "d"):
+                        st["vx"], st["vd"], st["vdone"] = self._get(st, "x"), self._get(st, "d"), st["done"]
+                    else:
+                        st["gerbicz_errors"] += 1
+                        self._set(st, "x", st["vx"])
+                        self._set(st, "d", st["vd"])
+                        st["done"] = st.get("vdone", 0)
+            finally:
+                for g in (gx, gd, gt):
+                    self.lib.kn_group_free(g)
+        return [{"k": st["k"], "n": st["n"], "res64": st["res64"], "is_prp": st["is_prp"],
+                 "gerbicz_errors": st["gerbicz_errors"]} for st in self.t]
+
+    def _corrupt(self, st):
+        v = self._get(st, "x")
+        self._set(st, "x", (v + (1 << (st["n"] // 3))) % st["N"])
+
+    def close(self):
+        for st in self.t:
+            for name in ("x", "d", "t", "x0"):
+                if st.get(name):
+                    self.lib.kn_num_free(st["e"], st[name])
+            self.lib.kn_engine_free(st["e"])
+        self.t = []
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
 def time_steps(tests, squarings: int = 64, reps: int = 3, device: int = 0):
     """(median seconds per squaring step of all tests, transform lengths)"""
     with NttGroup(tests, device) as g:

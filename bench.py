@@ -390,16 +390,20 @@ def large_segment(lib, seed=4, squarings=100_000, block=1000, blocks_per_check=5
             "stopped_on_request": rc == -5}
 
 
-def ntt_leg(lib, tests, mean_n, device, squarings=64, reps=3):
-    """The same tests on the exact integer-NTT engine (include/kite_ntt.h): one group, every
-    test's number squared `squarings` times per timed call (CUDA events on the group's stream).
-    tests/hour counts a Gerbicz block as B squarings plus one product, a product as two
-    squarings, and the check every M blocks, as the FP64 line does."""
-    from ahnum_gb300.ntt_group import time_steps
-    t_sq, nps = time_steps(tests, squarings, reps, device)
-    t_block = (BLOCK + 2) * t_sq
+def ntt_leg(lib, tests, mean_n, device, blocks=3):
+    """The same tests on the exact integer-NTT engine (include/kite_ntt.h): a lockstep Gerbicz
+    batch (ahnum_gb300.ntt_group.NttFermatBatch) of all tests, B = 1000, M = 250, timed over
+    `blocks` blocks of B squarings and the block product (CUDA events on the groups' streams);
+    tests/hour with the FP64 line's block accounting."""
+    from ahnum_gb300.ntt_group import NttFermatBatch, time_steps
+    with NttFermatBatch(tests, block=BLOCK, blocks_per_check=BLOCKS_PER_CHECK, device=device) as nb:
+        nb.run(max_blocks=1)  # graphs, clocks
+        nb.block_ms, nb.blocks = 0.0, 0
+        nb.run(max_blocks=blocks)
+        t_block = nb.block_ms * 1e-3 / nb.blocks
+    t_sq, nps = time_steps(tests, 64, 3, device)
     tph = 3600.0 * len(tests) * BLOCK / (t_block * (1 + 1 / BLOCKS_PER_CHECK) * mean_n)
-    return {"tests_per_hour": tph, "ms_per_squaring_step": t_sq * 1e3,
+    return {"tests_per_hour": tph, "ms_per_block": t_block * 1e3, "ms_per_squaring_step": t_sq * 1e3,
             "us_per_test_squaring": t_sq * 1e6 / len(tests),
             "transform_lengths": {str(k): v for k, v in nps.items()},
             "gpu_launches_per_squaring": 4,

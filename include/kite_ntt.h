@@ -67,6 +67,9 @@ kn_group *kn_group_new(int device);
 void kn_group_free(kn_group *g);
 int kn_group_add(kn_group *g, kn_engine *e, uint64_t *x);
 int kn_group_square(kn_group *g, uint64_t count, float *gpu_ms);
+/* Every member's number times ys[i] (members in the order they were added; ys[i] a number of
+ * member i's engine, distinct from its own number). */
+int kn_group_mul(kn_group *g, const uint64_t *const *ys, float *gpu_ms);
 int kn_group_error(const kn_group *g);
 
 #ifdef __cplusplus

@@ -198,3 +198,20 @@ def test_group_squares_every_member(lib):
         lib.kn_group_free(g)
         for e in engines:
             e.close()
+
+
+def test_ntt_fermat_batch_known_residues(lib):
+    """a lockstep Gerbicz batch on NTT groups: tests of different n leave the lockstep as they
+    near their end and finish alone; every RES64 equals the reference's known residue, and a
+    fault injected in one test is caught by its check and rolled back"""
+    from ahnum_gb300.ntt_group import NttFermatBatch
+    want = {(9357, 20000): 0x79291CD2F47CE48C, (3, 26459): 0x1, (1, 44497): 0x1,
+            (9999, 60000): 0x1C248905164FFD34, (1203, 90001): 0x4BE9F1953E350085}
+    with NttFermatBatch(list(want), block=1000, blocks_per_check=10) as b:
+        b.fault = (9999, 13000)
+        res = b.run()
+        assert b.blocks > 0 and b.block_ms > 0
+    for r in res:
+        assert r["res64"] == want[(r["k"], r["n"])], (r["k"], r["n"], hex(r["res64"]))
+        assert r["is_prp"] == (want[(r["k"], r["n"])] == 1)
+        assert r["gerbicz_errors"] == (1 if r["k"] == 9999 else 0)
