@@ -713,17 +713,22 @@ void sub_in(std::vector<uint64_t> &a, const std::vector<uint64_t> &b) {
     }
 }
 
+// The sizes of a number of the engine for N = k 2^n - 1 and the modulus itself: host-only.
+struct NumLayout {
+    uint64_t k = 0, n = 0;
+    uint32_t W = 0, w = 0, NP = 0;
+    size_t nlimbs = 0;
+    std::vector<uint64_t> N;  // modulus, nlimbs limbs
+    bool build(uint64_t k, uint64_t n);
+};
+
 }  // namespace kn
 
 using namespace kn;
 
-struct kn_engine {
+struct kn_engine : kn::NumLayout {
     int device = 0;
     cudaStream_t stream = nullptr;
-    uint64_t k = 0, n = 0;
-    uint32_t W = 0, w = 0, NP = 0;
-    size_t nlimbs = 0;
-    std::vector<uint64_t> N;         // modulus, nlimbs limbs (+1 spare)
     std::shared_ptr<Plan> plan;
     Desc desc{};
     Desc *d_desc = nullptr;
@@ -776,7 +781,7 @@ void limbs_to_words(const std::vector<uint64_t> &l, uint32_t W, uint32_t w, uint
 
 // v mod N for v of any size (limbs, little endian), using k 2^n == 1: v = T 2^n + L,
 // T = q k + r -> v == L + q + r 2^n
-void reduce_mod(const kn_engine *e, std::vector<uint64_t> v, std::vector<uint64_t> &out) {
+void reduce_mod(const NumLayout *e, std::vector<uint64_t> v, std::vector<uint64_t> &out) {
     const uint64_t n = e->n, k = e->k;
     for (;;) {
         // T = v >> n
@@ -826,7 +831,7 @@ void reduce_mod(const kn_engine *e, std::vector<uint64_t> v, std::vector<uint64_
 }
 
 // Montgomery form x~ = x 2^n mod N of x in [0, N): x = q k + r -> x 2^n == q + r 2^n
-void to_mont(const kn_engine *e, const uint64_t *limbs, std::vector<uint64_t> &out) {
+void to_mont(const NumLayout *e, const uint64_t *limbs, std::vector<uint64_t> &out) {
     std::vector<uint64_t> q(limbs, limbs + e->nlimbs);
     u128 rem = 0;
     for (size_t j = q.size(); j-- > 0;) {
@@ -845,7 +850,7 @@ void to_mont(const kn_engine *e, const uint64_t *limbs, std::vector<uint64_t> &o
 }
 
 // A constant c as Montgomery words (a representative in [0, N)).
-bool constant_words(kn_engine *e, int64_t c, std::vector<uint64_t> &words) {
+bool constant_words(const NumLayout *e, int64_t c, std::vector<uint64_t> &words) {
     std::vector<uint64_t> v(e->nlimbs, 0);
     if (c >= 0) {
         v[0] = (uint64_t)c;
@@ -908,26 +913,72 @@ bool prepare_smem(int device, size_t col_smem, size_t row_smem) {
     return ok;
 }
 
+// x~ (W words of w bits) -> x = x~ 2^-n = x~ k (mod N) as canonical limbs
+void from_mont(const NumLayout *e, const uint64_t *words, uint64_t *limbs) {
+    std::vector<uint64_t> v((size_t)e->W * e->w / 64 + 3, 0);
+    words_to_limbs(words, e->W, e->w, v);
+    u128 c = 0;
+    for (auto &l : v) {
+        c += (u128)l * e->k;
+        l = (uint64_t)c;
+        c >>= 64;
+    }
+    v.push_back((uint64_t)c);
+    std::vector<uint64_t> out;
+    reduce_mod(e, v, out);
+    std::copy(out.begin(), out.end(), limbs);
+}
+
 }  // namespace
+
+bool kn::NumLayout::build(uint64_t kk, uint64_t nn) {
+    if (!(kk & 1) || kk >= (1ull << 30) || nn < 8 || nn > (1ull << 26)) return false;
+    k = kk;
+    n = nn;
+    choose_sizes(k, n, w, W, NP);
+    if (!NP || NP > (1u << 20)) return false;
+    nlimbs = (size_t)((n + 64 + 63) / 64);
+    N = modulus(k, n, nlimbs);
+    return true;
+}
 
 extern "C" {
 
+int kn_layout(uint64_t k, uint64_t n, uint32_t *w, uint32_t *W, uint32_t *NP) {
+    NumLayout y;
+    if (!y.build(k, n)) return -1;
+    if (w) *w = y.w;
+    if (W) *W = y.W;
+    if (NP) *NP = y.NP;
+    return 0;
+}
+
+int kn_limbs_to_words(uint64_t k, uint64_t n, const uint64_t *limbs, uint64_t *words) {
+    NumLayout y;
+    if (!y.build(k, n)) return -1;
+    std::vector<uint64_t> mont;
+    to_mont(&y, limbs, mont);
+    limbs_to_words(mont, y.W, y.w, words);
+    return 0;
+}
+
+int kn_words_to_limbs(uint64_t k, uint64_t n, const uint64_t *words, uint64_t *limbs) {
+    NumLayout y;
+    if (!y.build(k, n)) return -1;
+    from_mont(&y, words, limbs);
+    return 0;
+}
+
 kn_engine *kn_engine_new(uint64_t k, uint64_t n, int device) {
-    if (!(k & 1) || k >= (1ull << 30) || n < 8 || n > (1ull << 26)) return nullptr;
     if (device < 0 && cudaGetDevice(&device) != cudaSuccess) return nullptr;
     if (cudaSetDevice(device) != cudaSuccess) return nullptr;
     kn_engine *e = new (std::nothrow) kn_engine();
     if (!e) return nullptr;
     e->device = device;
-    e->k = k;
-    e->n = n;
-    choose_sizes(k, n, e->w, e->W, e->NP);
-    if (!e->NP || e->NP > (1u << 20)) {
+    if (!e->build(k, n)) {
         delete e;
         return nullptr;
     }
-    e->nlimbs = (size_t)((n + 64 + 63) / 64);
-    e->N = modulus(k, n, e->nlimbs);
     e->plan = get_plan(device, e->NP);
     if (!e->plan) {
         delete e;
@@ -1057,19 +1108,7 @@ int kn_get_limbs(kn_engine *e, const uint64_t *x, uint64_t *limbs) {
         e->err = -100 - st;
         return -1;
     }
-    // x = x~ 2^-n = x~ k (mod N)
-    std::vector<uint64_t> v((size_t)e->W * e->w / 64 + 3, 0);
-    words_to_limbs(words.data(), e->W, e->w, v);
-    u128 c = 0;
-    for (auto &l : v) {
-        c += (u128)l * e->k;
-        l = (uint64_t)c;
-        c >>= 64;
-    }
-    v.push_back((uint64_t)c);
-    std::vector<uint64_t> out;
-    reduce_mod(e, v, out);
-    std::copy(out.begin(), out.end(), limbs);
+    from_mont(e, words.data(), limbs);
     return 0;
 }
 

@@ -57,6 +57,13 @@ int kn_copy(kn_engine *e, uint64_t *dst, const uint64_t *src);
 int kn_error(const kn_engine *e);
 int kn_sync(kn_engine *e);
 
+/* Host-only, no GPU needed: the engine's sizes for N = k*2^n - 1 (0, or -1 if out of range), and
+ * the conversions between a canonical value in [0, N) (kn_limbs-many limbs: (n + 127) / 64) and
+ * the engine's W words in Montgomery form x~ = x*2^n mod N. */
+int kn_layout(uint64_t k, uint64_t n, uint32_t *w, uint32_t *W, uint32_t *NP);
+int kn_limbs_to_words(uint64_t k, uint64_t n, const uint64_t *limbs, uint64_t *words);
+int kn_words_to_limbs(uint64_t k, uint64_t n, const uint64_t *words, uint64_t *limbs);
+
 /* Groups: one launch set per squaring advances every member at once (many tests on one GPU, as
  * the reference's prototype keeps B numbers in flight, gpu/gpu_ctx.h:57-77).  A member is an
  * engine with the number it squares; engines may differ in k and n but not repeat, since each
