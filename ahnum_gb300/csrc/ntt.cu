@@ -112,36 +112,46 @@ __device__ __forceinline__ int log2i(uint32_t x) { return 31 - __clz(x); }
 // e + (e >> log2 B) so that both access patterns are free of bank conflicts.
 //
 // DIF levels over register values at positions c0 + m*stride: level s pairs m with m + s/stride
-// and multiplies the difference by w_2s^(c mod s) = tw[s + (c mod s)].
-template <int A>
+// and multiplies the difference by w_2s^(c mod s) = tw[s + (c mod s)].  NARROW: stride 1 and c0 a
+// multiple of A, so c mod s = m mod s is known at compile time and the butterflies whose twiddle
+// is 1 (m mod s = 0: all of level 1, half of level 2, ...) skip the multiplication.
+template <int A, bool NARROW>
 __device__ __forceinline__ void dif_regs(uint32_t (&x)[A], int c0, int stride, const uint2 *tw, uint32_t p) {
     const uint32_t p2 = 2 * p;
 #pragma unroll
     for (int half = A / 2; half >= 1; half >>= 1) {
-        const int s = stride * half;
+        const int s = NARROW ? half : stride * half;
 #pragma unroll
         for (int m = 0; m < A; m++) {
             if (m & half) continue;
-            const int c = c0 + m * stride;
             const uint32_t u = x[m], v = x[m + half];
             x[m] = red2(u + v, p2);
-            x[m + half] = shoup(u - v + p2, __ldg(&tw[s + (c & (s - 1))]), p);
+            if (NARROW && (m & (half - 1)) == 0) {
+                x[m + half] = red2(u - v + p2, p2);
+            } else {
+                const int c = NARROW ? m : c0 + m * stride;
+                x[m + half] = shoup(u - v + p2, __ldg(&tw[s + (c & (s - 1))]), p);
+            }
         }
     }
 }
 
 // DIT levels (inverse), ascending: (u, v) -> (u + v w, u - v w), w = w_2s^-(c mod s)
-template <int A>
+template <int A, bool NARROW>
 __device__ __forceinline__ void dit_regs(uint32_t (&x)[A], int c0, int stride, const uint2 *tw, uint32_t p) {
     const uint32_t p2 = 2 * p;
 #pragma unroll
     for (int half = 1; half < A; half <<= 1) {
-        const int s = stride * half;
+        const int s = NARROW ? half : stride * half;
 #pragma unroll
         for (int m = 0; m < A; m++) {
             if (m & half) continue;
-            const int c = c0 + m * stride;
-            const uint32_t u = x[m], v = shoup(x[m + half], __ldg(&tw[s + (c & (s - 1))]), p);
+            const uint32_t u = x[m];
+            uint32_t v = x[m + half];
+            if (!(NARROW && (m & (half - 1)) == 0)) {
+                const int c = NARROW ? m : c0 + m * stride;
+                v = shoup(v, __ldg(&tw[s + (c & (s - 1))]), p);
+            }
             x[m] = red2(u + v, p2);
             x[m + half] = red2(u - v + p2, p2);
         }
@@ -176,7 +186,7 @@ __device__ __forceinline__ void col_fwd_item(uint32_t *sm, const Desc &D, int g,
         uint32_t x[A];
 #pragma unroll
         for (int m = 0; m < A; m++) x[m] = sm[col_addr<B>(i, RP, t + B * m, l)];
-        dif_regs<A>(x, t, B, D.tb.twr_f[i], D.pr[i].p);
+        dif_regs<A, false>(x, t, B, D.tb.twr_f[i], D.pr[i].p);
 #pragma unroll
         for (int m = 0; m < A; m++) sm[col_addr<B>(i, RP, t + B * m, l)] = x[m];
     }
@@ -186,7 +196,7 @@ __device__ __forceinline__ void col_fwd_item(uint32_t *sm, const Desc &D, int g,
         uint32_t x[B];
 #pragma unroll
         for (int m = 0; m < B; m++) x[m] = sm[col_addr<B>(i, RP, B * t2 + m, l)];
-        dif_regs<B>(x, B * t2, 1, D.tb.twr_f[i], D.pr[i].p);
+        dif_regs<B, true>(x, B * t2, 1, D.tb.twr_f[i], D.pr[i].p);
         const uint32_t p = D.pr[i].p;
 #pragma unroll
         for (int m = 0; m < B; m++) {
@@ -232,7 +242,7 @@ __device__ __forceinline__ void row_item(uint32_t *sm, const Desc &D, int pos) {
         uint32_t x[A];
 #pragma unroll
         for (int m = 0; m < A; m++) x[m] = src[base + B * m];
-        dif_regs<A>(x, t, B, D.tb.twc_f[i], D.pr[i].p);
+        dif_regs<A, false>(x, t, B, D.tb.twc_f[i], D.pr[i].p);
         uint32_t *row = sm + (op * kPrimes + i) * CP;
 #pragma unroll
         for (int m = 0; m < A; m++) row[t + B * m + m] = x[m];
@@ -246,20 +256,20 @@ __device__ __forceinline__ void row_item(uint32_t *sm, const Desc &D, int pos) {
         uint32_t x[B];
 #pragma unroll
         for (int m = 0; m < B; m++) x[m] = row[m];
-        dif_regs<B>(x, B * t2, 1, D.tb.twc_f[i], p);
+        dif_regs<B, true>(x, B * t2, 1, D.tb.twc_f[i], p);
         if (MUL) {
             const uint32_t *rowy = sm + (kPrimes + i) * CP + (B + 1) * t2;
             uint32_t y[B];
 #pragma unroll
             for (int m = 0; m < B; m++) y[m] = rowy[m];
-            dif_regs<B>(y, B * t2, 1, D.tb.twc_f[i], p);
+            dif_regs<B, true>(y, B * t2, 1, D.tb.twc_f[i], p);
 #pragma unroll
             for (int m = 0; m < B; m++) x[m] = montmul(x[m], y[m], p, pinv);
         } else {
 #pragma unroll
             for (int m = 0; m < B; m++) x[m] = montmul(x[m], x[m], p, pinv);
         }
-        dit_regs<B>(x, B * t2, 1, D.tb.twc_i[i], p);
+        dit_regs<B, true>(x, B * t2, 1, D.tb.twc_i[i], p);
 #pragma unroll
         for (int m = 0; m < B; m++) row[m] = x[m];
     }
@@ -271,7 +281,7 @@ __device__ __forceinline__ void row_item(uint32_t *sm, const Desc &D, int pos) {
         uint32_t x[A];
 #pragma unroll
         for (int m = 0; m < A; m++) x[m] = row[t + B * m + m];
-        dit_regs<A>(x, t, B, D.tb.twc_i[i], D.pr[i].p);
+        dit_regs<A, false>(x, t, B, D.tb.twc_i[i], D.pr[i].p);
         const size_t base = (size_t)i * D.NP + (size_t)pos * C + t;
 #pragma unroll
         for (int m = 0; m < A; m++) D.res[base + B * m] = x[m];
@@ -332,7 +342,7 @@ __device__ __forceinline__ void col_inv_item(uint32_t *sm, const Desc &D, int g)
             const uint32_t mm = (uint32_t)(B * t2 + m) * C + g * kG + l;
             x[m] = shoup(D.res[(size_t)i * D.NP + mm], __ldg(&D.tb.t4_i[i][mm]), p);
         }
-        dit_regs<B>(x, B * t2, 1, D.tb.twr_i[i], p);
+        dit_regs<B, true>(x, B * t2, 1, D.tb.twr_i[i], p);
 #pragma unroll
         for (int m = 0; m < B; m++) sm[col_addr<B>(i, RP, B * t2 + m, l)] = x[m];
     }
@@ -343,7 +353,7 @@ __device__ __forceinline__ void col_inv_item(uint32_t *sm, const Desc &D, int g)
         uint32_t x[A];
 #pragma unroll
         for (int m = 0; m < A; m++) x[m] = sm[col_addr<B>(i, RP, t + B * m, l)];
-        dit_regs<A>(x, t, B, D.tb.twr_i[i], D.pr[i].p);
+        dit_regs<A, false>(x, t, B, D.tb.twr_i[i], D.pr[i].p);
 #pragma unroll
         for (int m = 0; m < A; m++) sm[col_addr<B>(i, RP, t + B * m, l)] = x[m];
     }
