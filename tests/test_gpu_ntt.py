@@ -215,3 +215,21 @@ def test_ntt_fermat_batch_known_residues(lib):
         assert r["res64"] == want[(r["k"], r["n"])], (r["k"], r["n"], hex(r["res64"]))
         assert r["is_prp"] == (want[(r["k"], r["n"])] == 1)
         assert r["gerbicz_errors"] == (1 if r["k"] == 9999 else 0)
+
+
+LARGE = _load("chains_large.json")
+
+
+@pytest.mark.parametrize("c", LARGE, ids=[c["name"] for c in LARGE])
+def test_large_chain_matches_gmp(lib, c):
+    """the large single-test regime (n in [2e7, 2.5e7]): transform length 2^20, the 1024 x 1024
+    four-step, against GMP's chain"""
+    e = Engine(c["k"], c["n"])
+    try:
+        assert e.lib.kn_transform_len(e.h) == 1 << 20
+        x = e.num(_seeded_residue(c["x0_seed"], c["k"], c["n"]))
+        assert e.lib.kn_square(e.h, x, c["squarings"]) == 0
+        v = e.get(x)
+        assert hashlib.sha256(v.to_bytes(8 * _nlimbs(c["n"]), "little")).hexdigest() == c["sha256_limbs"]
+    finally:
+        e.close()
