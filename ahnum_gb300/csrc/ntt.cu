@@ -115,7 +115,9 @@ __device__ __forceinline__ int log2i(uint32_t x) { return 31 - __clz(x); }
 // and multiplies the difference by w_2s^(c mod s) = tw[s + (c mod s)].  NARROW: stride 1 and c0 a
 // multiple of A, so c mod s = m mod s is known at compile time and the butterflies whose twiddle
 // is 1 (m mod s = 0: all of level 1, half of level 2, ...) skip the multiplication.
-template <int A, bool NARROW>
+// UPPER_ZERO: the values at m >= A/2 are zero (the padding half of an acyclic product's input),
+// so the first level only multiplies: (u, 0) -> (u, u w).
+template <int A, bool NARROW, bool UPPER_ZERO = false>
 __device__ __forceinline__ void dif_regs(uint32_t (&x)[A], int c0, int stride, const uint2 *tw, uint32_t p) {
     const uint32_t p2 = 2 * p;
 #pragma unroll
@@ -124,6 +126,11 @@ __device__ __forceinline__ void dif_regs(uint32_t (&x)[A], int c0, int stride, c
 #pragma unroll
         for (int m = 0; m < A; m++) {
             if (m & half) continue;
+            if (UPPER_ZERO && half == A / 2) {
+                const int c = NARROW ? m : c0 + m * stride;
+                x[m + half] = shoup(x[m] + p2, __ldg(&tw[s + (c & (s - 1))]), p);
+                continue;
+            }
             const uint32_t u = x[m], v = x[m + half];
             x[m] = red2(u + v, p2);
             if (NARROW && (m & (half - 1)) == 0) {
@@ -173,7 +180,9 @@ template <int A, int B>
 __device__ __forceinline__ void col_fwd_item(uint32_t *sm, const Desc &D, int g, const uint64_t *src, uint32_t *dst) {
     constexpr int R = A * B, RP = R + R / B;
     const int C = (int)D.C;
-    for (int e = threadIdx.x; e < R * kG; e += blockDim.x) {
+    // NP >= 2W: the words at r C + c >= W, hence every row r >= R/2, are the product's zero
+    // padding; only the lower half is converted and stored
+    for (int e = threadIdx.x; e < (R / 2) * kG; e += blockDim.x) {
         const int r = e >> 3, l = e & 7;
         const uint32_t j = (uint32_t)r * C + g * kG + l;
         const uint64_t word = j < D.W ? src[j] : 0;
@@ -185,8 +194,8 @@ __device__ __forceinline__ void col_fwd_item(uint32_t *sm, const Desc &D, int g,
         const int l = u & 7, t = (u >> 3) & (B - 1), i = u >> (3 + clog2<B>());
         uint32_t x[A];
 #pragma unroll
-        for (int m = 0; m < A; m++) x[m] = sm[col_addr<B>(i, RP, t + B * m, l)];
-        dif_regs<A, false>(x, t, B, D.tb.twr_f[i], D.pr[i].p);
+        for (int m = 0; m < A / 2; m++) x[m] = sm[col_addr<B>(i, RP, t + B * m, l)];
+        dif_regs<A, false, true>(x, t, B, D.tb.twr_f[i], D.pr[i].p);
 #pragma unroll
         for (int m = 0; m < A; m++) sm[col_addr<B>(i, RP, t + B * m, l)] = x[m];
     }
