@@ -67,6 +67,7 @@ struct Crt {
 
 struct Desc {
     uint32_t NP, R, C;
+    uint32_t np;                // primes in use: 3, or 4 when the coefficients need them
     uint32_t W, w, WN0, BN0;    // words, word bits, n / w, n % w
     uint64_t k;
     uint64_t *x;                // operand and result
@@ -180,17 +181,17 @@ template <int A, int B>
 __device__ __forceinline__ void col_fwd_item(uint32_t *sm, const Desc &D, int g, const uint64_t *src, uint32_t *dst) {
     constexpr int R = A * B, RP = R + R / B;
     const int C = (int)D.C;
+    const int np = (int)D.np;
     // NP >= 2W: the words at r C + c >= W, hence every row r >= R/2, are the product's zero
     // padding; only the lower half is converted and stored
     for (int e = threadIdx.x; e < (R / 2) * kG; e += blockDim.x) {
         const int r = e >> 3, l = e & 7;
         const uint32_t j = (uint32_t)r * C + g * kG + l;
         const uint64_t word = j < D.W ? src[j] : 0;
-#pragma unroll
-        for (int i = 0; i < kPrimes; i++) sm[col_addr<B>(i, RP, r, l)] = residue(word, D.pr[i]);
+        for (int i = 0; i < np; i++) sm[col_addr<B>(i, RP, r, l)] = residue(word, D.pr[i]);
     }
     __syncthreads();
-    for (int u = threadIdx.x; u < kPrimes * B * kG; u += blockDim.x) {
+    for (int u = threadIdx.x; u < np * B * kG; u += blockDim.x) {
         const int l = u & 7, t = (u >> 3) & (B - 1), i = u >> (3 + clog2<B>());
         uint32_t x[A];
 #pragma unroll
@@ -200,7 +201,7 @@ __device__ __forceinline__ void col_fwd_item(uint32_t *sm, const Desc &D, int g,
         for (int m = 0; m < A; m++) sm[col_addr<B>(i, RP, t + B * m, l)] = x[m];
     }
     __syncthreads();
-    for (int u = threadIdx.x; u < kPrimes * A * kG; u += blockDim.x) {
+    for (int u = threadIdx.x; u < np * A * kG; u += blockDim.x) {
         const int l = u & 7, t2 = (u >> 3) & (A - 1), i = u >> (3 + clog2<A>());
         uint32_t x[B];
 #pragma unroll
@@ -243,22 +244,23 @@ template <int A, int B, bool MUL>
 __device__ __forceinline__ void row_item(uint32_t *sm, const Desc &D, int pos) {
     constexpr int C = A * B, CP = C + C / B, lB = clog2<B>(), lA = clog2<A>();
     constexpr int nops = MUL ? 2 : 1;
+    const int np = (int)D.np;
     // wide forward levels straight from global memory
-    for (int u = threadIdx.x; u < nops * kPrimes * B; u += blockDim.x) {
-        const int t = u & (B - 1), i = (u >> lB) & (kPrimes - 1), op = u >> (lB + 2);
+    for (int u = threadIdx.x; u < nops * np * B; u += blockDim.x) {
+        const int t = u & (B - 1), q = u >> lB, op = q >= np, i = q - op * np;
         const uint32_t *src = op ? D.res2 : D.res;
         const size_t base = (size_t)i * D.NP + (size_t)pos * C + t;
         uint32_t x[A];
 #pragma unroll
         for (int m = 0; m < A; m++) x[m] = src[base + B * m];
         dif_regs<A, false>(x, t, B, D.tb.twc_f[i], D.pr[i].p);
-        uint32_t *row = sm + (op * kPrimes + i) * CP;
+        uint32_t *row = sm + (op * np + i) * CP;
 #pragma unroll
         for (int m = 0; m < A; m++) row[t + B * m + m] = x[m];
     }
     __syncthreads();
     // narrow forward levels, the pointwise product, narrow inverse levels
-    for (int u = threadIdx.x; u < kPrimes * A; u += blockDim.x) {
+    for (int u = threadIdx.x; u < np * A; u += blockDim.x) {
         const int t2 = u & (A - 1), i = u >> lA;
         uint32_t *row = sm + i * CP + (B + 1) * t2;
         const uint32_t p = D.pr[i].p, pinv = D.pr[i].pinv;
@@ -267,7 +269,7 @@ __device__ __forceinline__ void row_item(uint32_t *sm, const Desc &D, int pos) {
         for (int m = 0; m < B; m++) x[m] = row[m];
         dif_regs<B, true>(x, B * t2, 1, D.tb.twc_f[i], p);
         if (MUL) {
-            const uint32_t *rowy = sm + (kPrimes + i) * CP + (B + 1) * t2;
+            const uint32_t *rowy = sm + (np + i) * CP + (B + 1) * t2;
             uint32_t y[B];
 #pragma unroll
             for (int m = 0; m < B; m++) y[m] = rowy[m];
@@ -284,7 +286,7 @@ __device__ __forceinline__ void row_item(uint32_t *sm, const Desc &D, int pos) {
     }
     __syncthreads();
     // wide inverse levels straight to global memory
-    for (int u = threadIdx.x; u < kPrimes * B; u += blockDim.x) {
+    for (int u = threadIdx.x; u < np * B; u += blockDim.x) {
         const int t = u & (B - 1), i = u >> lB;
         const uint32_t *row = sm + i * CP;
         uint32_t x[A];
@@ -328,6 +330,10 @@ __device__ __forceinline__ ulonglong2 garner(const uint32_t *v, const Desc &D) {
     const uint32_t x1 = red2(shoup(sub_mod(v[1], red2(x0, p1), p1), D.crt.inv01, p1), p1);
     uint32_t t = red2(shoup(sub_mod(v[2], red2(x0, p2), p2), D.crt.inv02, p2), p2);
     const uint32_t x2 = red2(shoup(sub_mod(t, red2(x1, p2), p2), D.crt.inv12, p2), p2);
+    if (D.np == 3) {  // c = x0 + p0 (x1 + p1 x2) < 2^90
+        const u128 c = (u128)x0 + (u128)p0 * ((u128)x1 + (u128)p1 * x2);
+        return make_ulonglong2((unsigned long long)c, (unsigned long long)(c >> 64));
+    }
     t = red2(shoup(sub_mod(v[3], red2(x0, p3), p3), D.crt.inv03, p3), p3);
     t = red2(shoup(sub_mod(t, red2(x1, p3), p3), D.crt.inv13, p3), p3);
     const uint32_t x3 = red2(shoup(sub_mod(t, red2(x2, p3), p3), D.crt.inv23, p3), p3);
@@ -340,9 +346,9 @@ __device__ __forceinline__ ulonglong2 garner(const uint32_t *v, const Desc &D) {
 template <int A, int B>
 __device__ __forceinline__ void col_inv_item(uint32_t *sm, const Desc &D, int g) {
     constexpr int R = A * B, RP = R + R / B;
-    const int C = (int)D.C;
+    const int C = (int)D.C, np = (int)D.np;
     // narrow inverse levels straight from global memory, after the inverse four-step twiddle
-    for (int u = threadIdx.x; u < kPrimes * A * kG; u += blockDim.x) {
+    for (int u = threadIdx.x; u < np * A * kG; u += blockDim.x) {
         const int l = u & 7, t2 = (u >> 3) & (A - 1), i = u >> (3 + clog2<A>());
         const uint32_t p = D.pr[i].p;
         uint32_t x[B];
@@ -357,7 +363,7 @@ __device__ __forceinline__ void col_inv_item(uint32_t *sm, const Desc &D, int g)
     }
     __syncthreads();
     // wide inverse levels
-    for (int u = threadIdx.x; u < kPrimes * B * kG; u += blockDim.x) {
+    for (int u = threadIdx.x; u < np * B * kG; u += blockDim.x) {
         const int l = u & 7, t = (u >> 3) & (B - 1), i = u >> (3 + clog2<B>());
         uint32_t x[A];
 #pragma unroll
@@ -378,7 +384,7 @@ __device__ __forceinline__ void col_inv_item(uint32_t *sm, const Desc &D, int g)
         const int r = e >> 3, l = e & 7;
         uint32_t v[kPrimes];
 #pragma unroll
-        for (int i = 0; i < kPrimes; i++) v[i] = red2(sm[col_addr<B>(i, RP, r, l)], D.pr[i].p);
+        for (int i = 0; i < kPrimes; i++) v[i] = i < np ? red2(sm[col_addr<B>(i, RP, r, l)], D.pr[i].p) : 0;
         const ulonglong2 c2 = garner(v, D);
         const u128 c = ((u128)c2.y << 64) | c2.x;
         const uint64_t lo = (uint64_t)c & M, mid = (uint64_t)(c >> w) & M;
@@ -735,7 +741,7 @@ void sub_in(std::vector<uint64_t> &a, const std::vector<uint64_t> &b) {
 // The sizes of a number of the engine for N = k 2^n - 1 and the modulus itself: host-only.
 struct NumLayout {
     uint64_t k = 0, n = 0;
-    uint32_t W = 0, w = 0, NP = 0;
+    uint32_t np = 0, W = 0, w = 0, NP = 0;
     size_t nlimbs = 0;
     std::vector<uint64_t> N;  // modulus, nlimbs limbs
     bool build(uint64_t k, uint64_t n);
@@ -888,26 +894,35 @@ bool constant_words(const NumLayout *e, int64_t c, std::vector<uint64_t> &words)
     return true;
 }
 
-// transform length and word size for n: the largest w <= 50 whose coefficients stay below the
-// primes' product, among those that give the smallest power-of-2 length >= 2W
-void choose_sizes(uint64_t k, uint64_t n, uint32_t &w, uint32_t &W, uint32_t &NP) {
+// Primes, word size and transform length for n: the fewest prime-points (primes x NP, NP the
+// shortest power-of-2 length >= 2W), then the largest word w <= 50, subject to every convolution
+// coefficient staying below the product of the primes in use (W (2^w - 1)^2 < p_0 ... p_(np-1))
+// and W w leaving room for n + 2 log2 k + 8 bits.
+void choose_sizes(uint64_t k, uint64_t n, uint32_t &np, uint32_t &w, uint32_t &W, uint32_t &NP) {
     int kb = 0;
     while (kb < 63 && (k >> kb) > 0) kb++;
     const uint64_t bits = n + 2 * (uint64_t)kb + 8;
-    uint32_t best_np = 0;
-    for (uint32_t ww = 50; ww >= 24; ww--) {
-        const uint64_t Wc = (bits + ww - 1) / ww;
-        const int lw = ilog2((uint32_t)Wc);
-        if (2 * ww + lw + 1 > 119) continue;
-        uint64_t np = 64;
-        while (np < 2 * Wc) np <<= 1;
-        if (!best_np || np < best_np) {
-            best_np = (uint32_t)np;
-            w = ww;
-            W = (uint32_t)Wc;
+    uint64_t best = 0;
+    NP = 0;
+    for (uint32_t q = 3; q <= (uint32_t)kPrimes; q++) {
+        u128 prod = 1;
+        for (uint32_t i = 0; i < q; i++) prod *= kP[i];
+        for (uint32_t ww = 50; ww >= 24; ww--) {
+            const uint64_t Wc = (bits + ww - 1) / ww;
+            const u128 bound = (u128)Wc * (((u128)1 << ww) - 1) * (((u128)1 << ww) - 1);
+            if (bound >= prod) continue;
+            uint64_t len = 64;
+            while (len < 2 * Wc) len <<= 1;
+            const uint64_t cost = len * q;
+            if (!best || cost < best) {
+                best = cost;
+                np = q;
+                w = ww;
+                W = (uint32_t)Wc;
+                NP = (uint32_t)len;
+            }
         }
     }
-    NP = best_np;
 }
 
 // The dynamic shared-memory limit is a per-kernel property of the device's context, shared by
@@ -954,7 +969,7 @@ bool kn::NumLayout::build(uint64_t kk, uint64_t nn) {
     if (!(kk & 1) || kk >= (1ull << 30) || nn < 8 || nn > (1ull << 26)) return false;
     k = kk;
     n = nn;
-    choose_sizes(k, n, w, W, NP);
+    choose_sizes(k, n, np, w, W, NP);
     if (!NP || NP > (1u << 20)) return false;
     nlimbs = (size_t)((n + 64 + 63) / 64);
     N = modulus(k, n, nlimbs);
@@ -963,9 +978,10 @@ bool kn::NumLayout::build(uint64_t kk, uint64_t nn) {
 
 extern "C" {
 
-int kn_layout(uint64_t k, uint64_t n, uint32_t *w, uint32_t *W, uint32_t *NP) {
+int kn_layout(uint64_t k, uint64_t n, uint32_t *primes, uint32_t *w, uint32_t *W, uint32_t *NP) {
     NumLayout y;
     if (!y.build(k, n)) return -1;
+    if (primes) *primes = y.np;
     if (w) *w = y.w;
     if (W) *W = y.W;
     if (NP) *NP = y.NP;
@@ -1032,6 +1048,7 @@ kn_engine *kn_engine_new(uint64_t k, uint64_t n, int device) {
     }
     Desc &d = e->desc;
     d.NP = NP;
+    d.np = e->np;
     d.R = R;
     d.C = C;
     d.W = e->W;

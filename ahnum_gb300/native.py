@@ -190,7 +190,7 @@ PROTOTYPES = {
     "kn_copy": (C.c_int, [vp, vp, vp]),
     "kn_error": (C.c_int, [vp]),
     "kn_sync": (C.c_int, [vp]),
-    "kn_layout": (C.c_int, [C.c_uint64, C.c_uint64, u32p, u32p, u32p]),
+    "kn_layout": (C.c_int, [C.c_uint64, C.c_uint64, u32p, u32p, u32p, u32p]),
     "kn_limbs_to_words": (C.c_int, [C.c_uint64, C.c_uint64, u64p, u64p]),
     "kn_words_to_limbs": (C.c_int, [C.c_uint64, C.c_uint64, u64p, u64p]),
     "kn_group_new": (vp, [C.c_int]),

@@ -9,9 +9,10 @@
  * pipes, which GB300 has far more of than FP64 units.
  *
  * Representation: a number is W words of w bits (w <= 50) in 64-bit little-endian slots, value
- * x~ = x*2^n mod N up to a small multiple of N.  Four primes p < 2^30 with 2^20 | p-1; the
- * transform length NP is a power of 2 >= 2W; every convolution coefficient is below
- * W*2^(2w) < p0*p1*p2*p3, so the CRT recovers it exactly.
+ * x~ = x*2^n mod N up to a small multiple of N.  Three or four primes p < 2^30 with 2^20 | p-1 (per
+ * n, whichever needs fewer prime-points); the transform length NP is a power of 2 >= 2W; every
+ * convolution coefficient is below W*2^(2w) < the primes' product, so the CRT recovers it
+ * exactly.
  *
  * Numbers live in device memory.  Operations queue on the engine's stream; kn_get_limbs and
  * kn_sync wait.  A CUDA failure is sticky: kn_error returns it and later calls do nothing.
@@ -57,10 +58,11 @@ int kn_copy(kn_engine *e, uint64_t *dst, const uint64_t *src);
 int kn_error(const kn_engine *e);
 int kn_sync(kn_engine *e);
 
-/* Host-only, no GPU needed: the engine's sizes for N = k*2^n - 1 (0, or -1 if out of range), and
- * the conversions between a canonical value in [0, N) (kn_limbs-many limbs: (n + 127) / 64) and
- * the engine's W words in Montgomery form x~ = x*2^n mod N. */
-int kn_layout(uint64_t k, uint64_t n, uint32_t *w, uint32_t *W, uint32_t *NP);
+/* Host-only, no GPU needed: the engine's sizes for N = k*2^n - 1 -- the primes in use (3 or 4: the
+ * choice with the fewest prime-points), the word size, the words, the transform length -- (0, or -1
+ * if out of range), and the conversions between a canonical value in [0, N) (kn_limbs-many limbs:
+ * (n + 127) / 64) and the engine's W words in Montgomery form x~ = x*2^n mod N. */
+int kn_layout(uint64_t k, uint64_t n, uint32_t *primes, uint32_t *w, uint32_t *W, uint32_t *NP);
 int kn_limbs_to_words(uint64_t k, uint64_t n, const uint64_t *limbs, uint64_t *words);
 int kn_words_to_limbs(uint64_t k, uint64_t n, const uint64_t *words, uint64_t *limbs);
 

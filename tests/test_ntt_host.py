@@ -8,42 +8,56 @@ import random
 import pytest
 
 PRIMES = (1053818881, 975175681, 943718401, 880803841)
-PRODUCT = PRIMES[0] * PRIMES[1] * PRIMES[2] * PRIMES[3]
+
+
+def _product(q):
+    out = 1
+    for p in PRIMES[:q]:
+        out *= p
+    return out
 
 SIZES = [(3, 8), (3, 64), (1, 44497), (9357, 20000), (1203, 90001), (4733, 369717), (9999, 662695),
          ((1 << 30) - 1, 20011), (187, 24715281)]
 
 
 def _layout(lib, k, n):
-    w, W, NP = C.c_uint32(), C.c_uint32(), C.c_uint32()
-    assert lib.kn_layout(k, n, C.byref(w), C.byref(W), C.byref(NP)) == 0
-    return w.value, W.value, NP.value
+    q, w, W, NP = C.c_uint32(), C.c_uint32(), C.c_uint32(), C.c_uint32()
+    assert lib.kn_layout(k, n, C.byref(q), C.byref(w), C.byref(W), C.byref(NP)) == 0
+    return q.value, w.value, W.value, NP.value
 
 
 @pytest.mark.parametrize("k,n", SIZES)
 def test_sizes_bound_the_coefficients(lib, k, n):
-    w, W, NP = _layout(lib, k, n)
-    assert 24 <= w <= 50
+    q, w, W, NP = _layout(lib, k, n)
+    assert q in (3, 4) and 24 <= w <= 50
     assert W * w >= n + 2 * k.bit_length() + 8       # room for values below (k + 1) 2^n, squared
     assert NP >= 2 * W and NP & (NP - 1) == 0 and NP <= 1 << 20
-    assert W * ((1 << w) - 1) ** 2 < PRODUCT       # the CRT recovers every coefficient
-    # no shorter power-of-2 transform exists for any admissible word size
-    for ww in range(24, 51):
-        WW = -(-(n + 2 * k.bit_length() + 8) // ww)
-        if 2 * ww + (WW - 1).bit_length() + 1 <= 119:
-            assert NP <= max(64, 1 << (2 * WW - 1).bit_length())
+    assert W * ((1 << w) - 1) ** 2 < _product(q)   # the CRT recovers every coefficient
+    # no choice of primes and admissible word size needs fewer prime-points
+    for qq in (3, 4):
+        for ww in range(24, 51):
+            WW = -(-(n + 2 * k.bit_length() + 8) // ww)
+            if WW * ((1 << ww) - 1) ** 2 < _product(qq):
+                assert q * NP <= qq * max(64, 1 << (2 * WW - 1).bit_length())
+
+
+def test_three_primes_where_they_save_work(lib):
+    """n near 5e5: four primes need a 2^15 transform (w = 50), three primes (w <= 36) too, so
+    three are chosen; near 3.5e5 four primes fit 2^14 and are kept"""
+    assert _layout(lib, 4733, 500001)[0] == 3
+    assert _layout(lib, 4733, 369717)[0] == 4
 
 
 def test_out_of_range_refused(lib):
     w = C.c_uint32()
-    assert lib.kn_layout(4, 1000, C.byref(w), None, None) != 0      # k even
-    assert lib.kn_layout(1 << 30, 1000, None, None, None) != 0      # k too large
-    assert lib.kn_layout(3, 7, None, None, None) != 0               # n too small
+    assert lib.kn_layout(4, 1000, None, C.byref(w), None, None) != 0      # k even
+    assert lib.kn_layout(1 << 30, 1000, None, None, None, None) != 0      # k too large
+    assert lib.kn_layout(3, 7, None, None, None, None) != 0               # n too small
 
 
 @pytest.mark.parametrize("k,n", SIZES[:7])
 def test_montgomery_words_round_trip(lib, k, n):
-    w, W, NP = _layout(lib, k, n)
+    q, w, W, NP = _layout(lib, k, n)
     N = k * (1 << n) - 1
     nl = (n + 127) // 64
     rng = random.Random(k * 7919 + n)
@@ -65,7 +79,7 @@ def test_words_to_limbs_reduces_any_representative(lib):
     """the engine's results are Montgomery representatives below about (k + 1) 2^n: the
     conversion back reduces them fully"""
     k, n = 9357, 20000
-    w, W, NP = _layout(lib, k, n)
+    q, w, W, NP = _layout(lib, k, n)
     N = k * (1 << n) - 1
     nl = (n + 127) // 64
     rng = random.Random(5)
