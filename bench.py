@@ -407,7 +407,7 @@ def ntt_leg(lib, tests, mean_n, device, blocks=3):
             "us_per_test_squaring": t_sq * 1e6 / len(tests),
             "transform_lengths": {str(k): v for k, v in nps.items()},
             "gpu_launches_per_squaring": 4,
-            "arithmetic": "exact: residues mod four 30-bit primes, Garner CRT, Montgomery R=2^n"}
+            "arithmetic": "exact: residues mod three or four 30-bit primes, Garner CRT, Montgomery R=2^n"}
 
 
 _len_cache = {}
