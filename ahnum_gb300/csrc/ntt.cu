@@ -433,12 +433,18 @@ __global__ void __launch_bounds__(kColThreads) kn_col_inv(const Desc *descs, con
 
 // Carries pending at chunk boundaries: co[t] is the carry out of chunk t (S words at t S) into
 // chunk t + 1.  Adds them in until none is left; returns (in every thread) the carry that left
-// the top of v.
-__device__ u128 resolve_chunks(uint64_t *v, uint32_t len, uint32_t S, uint32_t w, u128 *co, u128 *top) {
+// the top of v.  A carry moves up at least one chunk per round, so T + 1 rounds always suffice;
+// the loop stops there in any case and reports bit 4 in *status if carries were still pending.
+__device__ u128 resolve_chunks(uint64_t *v, uint32_t len, uint32_t S, uint32_t w, u128 *co, u128 *top,
+                               int *status) {
     const int t = threadIdx.x, T = blockDim.x;
     const uint64_t M = (w == 64) ? ~0ull : ((1ull << w) - 1);
     if (t == 0) *top = 0;
-    for (;;) {
+    for (int round = 0;; round++) {
+        if (round > T + 1) {
+            if (t == 0) atomicOr(status, 4);
+            break;
+        }
         __syncthreads();
         const u128 cin = t > 0 ? co[t - 1] : 0;
         if (t == T - 1) *top += co[T - 1];
@@ -499,7 +505,7 @@ __global__ void __launch_bounds__(kReduceThreads) kn_reduce(const Desc *descs, c
             acc += ((u128)c.y << 64) | c.x;
         }
         co[t] = acc;
-        if (resolve_chunks(pw, NP, per << 3, w, co, &top) != 0 && t == 0) atomicOr(status, 1);
+        if (resolve_chunks(pw, NP, per << 3, w, co, &top, status) != 0 && t == 0) atomicOr(status, 1);
     }
     // 2. Montgomery reduction E = B + k A (+ addend), P = A + B 2^n
     {
@@ -530,7 +536,7 @@ __global__ void __launch_bounds__(kReduceThreads) kn_reduce(const Desc *descs, c
             }
         }
         co[t] = acc;
-        if (resolve_chunks(X, Wn, S, w, co, &top) != 0 && t == 0) atomicOr(status, 2);
+        if (resolve_chunks(X, Wn, S, w, co, &top, status) != 0 && t == 0) atomicOr(status, 2);
     }
     // 3. top fold: T = x >> n = q k + r; x <- x mod 2^n + q + r 2^n
     if (t == 0) {

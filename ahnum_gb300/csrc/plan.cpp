@@ -109,8 +109,41 @@ static int radix_stages(uint32_t n) {
     return st;
 }
 
+// Latency shapes chosen by the autotuner (or a tuning file), by FFT length L = 2H: (R, G).
+static std::map<uint32_t, std::pair<uint32_t, int>> g_latency;
+
+// the carry into a segment must be absorbed by 2g-1 digits of at least min_bits (a product's
+// carry stays below 2^(51 - b)), and the top region must fit one segment
+static bool group_fits(int g, unsigned min_bits, unsigned top_digits) {
+    return (2 * g - 1) * (int)min_bits >= 51 - (int)min_bits && (int)top_digits <= 2 * g;
+}
+
+bool set_latency_override(uint32_t L, uint32_t R, int G) {
+    std::lock_guard<std::mutex> lock(g_shape_mu);
+    if (!R) {
+        g_latency.erase(L);
+        return true;
+    }
+    if (L % 2 || (L / 2) % R || !shape_usable(L / 2, R, L / 2 / R) || (G != 2 && G != 4 && G != 8) ||
+        (L / 2 / R) % G)
+        return false;
+    g_latency[L] = {R, G};
+    return true;
+}
+
 bool choose_latency_shape(uint32_t H, int nsm, unsigned min_bits, unsigned top_digits, uint32_t &R,
                           uint32_t &C, int &G) {
+    {
+        // an autotuned shape of this length, where this number's digits allow its groups
+        std::lock_guard<std::mutex> lock(g_shape_mu);
+        auto it = g_latency.find(2 * H);
+        if (it != g_latency.end() && group_fits(it->second.second, min_bits, top_digits)) {
+            R = it->second.first;
+            C = H / R;
+            G = it->second.second;
+            return true;
+        }
+    }
     // FP64 lane-operations per point of each pass (measured: rows ~53, each column pass ~24),
     // a fixed cost per stage barrier, and the load of the busiest SM.
     double best = 1e300;
@@ -121,9 +154,7 @@ bool choose_latency_shape(uint32_t H, int nsm, unsigned min_bits, unsigned top_d
         if (H % c || !shape_usable(H, H / c, c)) continue;
         const uint32_t r = H / c;
         for (int g : {2, 4, 8}) {
-            // the carry into a segment must be absorbed by 2g-1 digits of at least min_bits (a
-            // product's carry stays below 2^(51 - b)), and the top region must fit one segment
-            if ((2 * g - 1) * (int)min_bits < 51 - (int)min_bits || (int)top_digits > 2 * g) continue;
+            if (!group_fits(g, min_bits, top_digits)) continue;
             const double pairs = r / 2 + 1, groups = c / g;
             const double rows = std::ceil(pairs / nsm) * 106.0 * c + 800.0 * (2 * radix_stages(c) + 2);
             const double cols = std::ceil(groups / nsm) * 24.0 * r * g + 800.0 * (radix_stages(r) + 2);

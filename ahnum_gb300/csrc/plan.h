@@ -41,8 +41,13 @@ double2 cis_neg(uint64_t j, uint64_t m);
 // Shape and column-group width for one test run alone: spread every pass over the SMs so the
 // squaring's latency, not its total FP64 work, is smallest.  Throughput (batched) use takes
 // choose_shape and G = kGroup instead.  min_bits: the narrowest digit; top_digits: L - top_t.
+// An autotuned shape of the length (set_latency_override) comes first wherever the number's
+// digits allow its group width.
 bool choose_latency_shape(uint32_t H, int nsm, unsigned min_bits, unsigned top_digits, uint32_t &R,
                           uint32_t &C, int &G);
+// Use R rows and column groups of G for one test alone at FFT length L from now on (R = 0: back
+// to the model); false if the shape is unusable.
+bool set_latency_override(uint32_t L, uint32_t R, int G);
 
 // Cached plan for (current device, L, R) (R = 0: choose_shape); nullptr if L cannot be planned or
 // the device upload fails.  Thread-safe.

@@ -14,6 +14,8 @@ extern "C" {
 
 int kc_set_fft_shape(uint32_t L, uint32_t R) { return kg::set_shape_override(L, R) ? 0 : -1; }
 
+int kc_set_latency_shape(uint32_t L, uint32_t R, int G) { return kg::set_latency_override(L, R, G) ? 0 : -1; }
+
 void kc_set_fft_time(uint32_t L, double us) { kg::set_tuned_time(L, us); }
 
 int kc_fft_shape_candidates(uint32_t L, uint32_t *R, uint32_t *C, int max) {
@@ -36,11 +38,16 @@ int kc_tuning_load(const char *path) {
     int count = 0;
     while (std::fgets(line, sizeof line, f)) {
         unsigned L = 0, R = 0, C = 0;
+        int G = 0;
         double us = 0;
-        int got = std::sscanf(line, "%u %lf %u %u", &L, &us, &R, &C);
+        int got = std::sscanf(line, "%u %lf %u %u %d", &L, &us, &R, &C, &G);
         if (got < 2 || line[0] == '#') continue;
-        if (us > 0) kg::set_tuned_time(L, us);
-        if (got == 4 && (uint64_t)R * C == L / 2) kg::set_shape_override(L, R);
+        if (got == 5) {
+            if ((uint64_t)R * C == L / 2) kg::set_latency_override(L, R, G);
+        } else {
+            if (us > 0) kg::set_tuned_time(L, us);
+            if (got == 4 && (uint64_t)R * C == L / 2) kg::set_shape_override(L, R);
+        }
         count++;
     }
     std::fclose(f);

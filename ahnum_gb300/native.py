@@ -166,6 +166,7 @@ PROTOTYPES = {
     "kc_set_fft_time": (None, [C.c_uint32, C.c_double]),
     "kc_fft_shape_candidates": (C.c_int, [C.c_uint32, u32p, u32p, C.c_int]),
     "kc_fft_shape": (C.c_int, [C.c_uint32, u32p, u32p]),
+    "kc_set_latency_shape": (C.c_int, [C.c_uint32, C.c_uint32, C.c_int]),
     "kc_tuning_load": (C.c_int, [C.c_char_p]),
     "kc_roundoff_probe": (C.c_double, [C.c_uint64, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint64]),
     "kc_layout": (C.c_int, [C.c_uint64, C.c_uint64, C.c_uint32, u8p, dp, dp, u64p]),

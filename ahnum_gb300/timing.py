@@ -5,7 +5,7 @@ measures on the CPU, tools/kite.c).
 
 squares 3 modulo N = K*2^N-1 W times, then S times, and prints the microseconds per squaring
 (wall clock around kite_square_n, synchronised) with the transform length and round-off as one
-JSON line.
+JSON line.  The shipped GB300 shapes (ahnum_gb300/tuning_gb300*.txt) are applied first.
 """
 from __future__ import annotations
 
@@ -13,11 +13,14 @@ import argparse
 import json
 import time
 
+from . import native
 from .kite import CUDA, CUDA_NTT, Ctx
+from .tune import load_gb300_tuning
 
 
 def time_single(k: int, n: int, fft_len: int = 0, squarings: int = 200, warmup: int = 20,
                 backend: int = CUDA) -> dict:
+    load_gb300_tuning(native.load())
     with Ctx(k, n, fft_len, backend=backend) as c:
         x = c.num(3)
         c.square(x, warmup)

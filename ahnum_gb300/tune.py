@@ -9,6 +9,13 @@
       also steer the length choice among safe lengths within 30 %, as the reference's tuning file
       does.
 
+  python -m ahnum_gb300.tune latency K:N [K:N ...] [--out FILE]
+      For each number, at the length the reference's chooser gives it: time every usable
+      four-step shape H = R*C with every column-group width G in {2, 4, 8} for one test run alone
+      (kc_engine_new, squarings queued back to back, wall clock around them) and keep the
+      fastest.  Writes "L us R C G" lines (kc_tuning_load reads them as latency shapes); the
+      built-in model's own choice is timed first and kept unless a shape beats it.
+
   python -m ahnum_gb300.tune roundoff L1 L2 ... [--k K] [--squarings S]
       For each length, the largest round-off over S squarings of a seeded residue at the largest
       n the reference's length model assigns to it for multiplier K (and at +0.25 and +0.5 bits
@@ -19,10 +26,34 @@ from __future__ import annotations
 import argparse
 import ctypes as C
 import math
+import os
 import sys
 
 from . import native
 from .kite import Batch
+
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+THROUGHPUT_FILE = os.path.join(HERE, "tuning_gb300.txt")
+LATENCY_FILE = os.path.join(HERE, "tuning_gb300_latency.txt")
+
+
+def load_gb300_tuning(lib) -> None:
+    """Applies the shipped GB300 shapes: the batched four-step shapes (shapes only: the FFT
+    lengths stay the ones the reference's length chooser picks without a times file) and the
+    single-test latency shapes."""
+    if os.path.exists(THROUGHPUT_FILE):
+        with open(THROUGHPUT_FILE) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) == 4 and not line.startswith("#"):
+                    lib.kc_set_fft_shape(int(parts[0]), int(parts[2]))
+    if os.path.exists(LATENCY_FILE):
+        with open(LATENCY_FILE) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) == 5 and not line.startswith("#"):
+                    lib.kc_set_latency_shape(int(parts[0]), int(parts[2]), int(parts[4]))
 
 
 def usable_lengths(lo: int, hi: int):
@@ -81,6 +112,90 @@ def tune_shapes(lengths, slots: int = 48, squarings: int = 64, out=None, log=sys
     return results
 
 
+def latency_shapes(L: int):
+    """Every usable (R, C) of H = L/2 for a test run alone: C a multiple of 8 in [16, 2048],
+    R in [2, 1024], both with prime factors 2, 3, 5, 7 only."""
+    H = L // 2
+    out = []
+    for c in range(16, 2049, 8):
+        if H % c:
+            continue
+        r = H // c
+        if 2 <= r <= 1024 and all(_smooth(v) for v in (r, c)):
+            out.append((r, c))
+    return out
+
+
+def _smooth(v: int) -> bool:
+    for p in (2, 3, 5, 7):
+        while v % p == 0:
+            v //= p
+    return v == 1
+
+
+def time_latency(lib, k: int, n: int, L: int, squarings: int, warmup: int = 20):
+    """(microseconds per squaring, R, C, G) of one test alone with the shape the library picks
+    now; None if the engine cannot be made."""
+    import time
+    e = lib.kc_engine_new(k, n, L, None, None, None, 0, 0, 0, 0, -1)
+    if not e:
+        return None
+    try:
+        R, Cc = C.c_uint32(), C.c_uint32()
+        lib.kc_shape(e, C.byref(R), C.byref(Cc))
+        G = lib.kc_group_width(e)
+        x = lib.kc_num_alloc(e)
+        digits = (C.c_int64 * L)()
+        digits[0] = 3
+        if not x or lib.kc_from_digits(e, x, digits) != 0:
+            return None
+        lib.kc_square(e, x, warmup)
+        lib.kc_sync(e)
+        t0 = time.perf_counter()
+        lib.kc_square(e, x, squarings)
+        rc = lib.kc_sync(e)
+        dt = time.perf_counter() - t0
+        lib.kc_num_free(e, x)
+        if rc != 0:
+            return None
+        return dt / squarings * 1e6, R.value, Cc.value, G
+    finally:
+        lib.kc_engine_free(e)
+
+
+def tune_latency(numbers, squarings: int = 200, out=None, log=sys.stderr):
+    lib = native.load()
+    results = []
+    for k, n in numbers:
+        L = lib.kc_choose_fft_len(k, n)
+        lib.kc_set_latency_shape(L, 0, 0)
+        model = time_latency(lib, k, n, L, squarings)
+        if model is None:
+            print(f"  {k}*2^{n}-1: no engine at L={L}", file=log, flush=True)
+            continue
+        print(f"  L={L} model R={model[1]} C={model[2]} G={model[3]}: {model[0]:.2f} us/sq",
+              file=log, flush=True)
+        best = model
+        for R, Cc in latency_shapes(L):
+            for G in (2, 4, 8):
+                if Cc % G or lib.kc_set_latency_shape(L, R, G) != 0:
+                    continue
+                t = time_latency(lib, k, n, L, squarings)
+                lib.kc_set_latency_shape(L, 0, 0)
+                if t is None or (t[1], t[3]) != (R, G):
+                    continue  # this number's digits do not allow groups of G
+                print(f"  L={L} R={R} C={Cc} G={G}: {t[0]:.2f} us/sq", file=log, flush=True)
+                best = min(best, t)
+        lib.kc_set_latency_shape(L, best[1], best[3])
+        results.append((L,) + best)
+        line = f"{L} {best[0]:.3f} {best[1]} {best[2]} {best[3]}"
+        print(line, flush=True)
+        if out:
+            out.write(line + "\n")
+            out.flush()
+    return results
+
+
 def roundoff_report(lengths, k: int = 9999, squarings: int = 500, seed: int = 1):
     lib = native.load()
     rows = []
@@ -104,6 +219,10 @@ def main():
     a.add_argument("--out")
     a.add_argument("--slots", type=int, default=48)
     a.add_argument("--squarings", type=int, default=64)
+    c = sub.add_parser("latency")
+    c.add_argument("numbers", nargs="+", help="K:N pairs")
+    c.add_argument("--squarings", type=int, default=200)
+    c.add_argument("--out")
     b = sub.add_parser("roundoff")
     b.add_argument("lengths", type=int, nargs="+")
     b.add_argument("--k", type=int, default=9999)
@@ -116,6 +235,14 @@ def main():
             if args.lengths:
                 Ls = [L for L in Ls if L in set(args.lengths)]
             tune_shapes(Ls, args.slots, args.squarings, out)
+        finally:
+            if out:
+                out.close()
+    elif args.cmd == "latency":
+        out = open(args.out, "w") if args.out else None
+        try:
+            nums = [tuple(int(v) for v in a.split(":")) for a in args.numbers]
+            tune_latency(nums, args.squarings, out)
         finally:
             if out:
                 out.close()

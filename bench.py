@@ -180,6 +180,14 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# DRAM bytes (read + write) of one k_rows launch over this workload's 256 tests, from an ncu
+# capture of the same launch: ncu --set full --clock-control none -k regex:k_rows -s 2 -c 1
+# python bench.py --quick --steps 1 --warmup 1 --no-ntt (76.47 MB read + 19.67 MB written)
+K_ROWS_DRAM_BYTES = 96.14e6
+K_ROWS_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_rows launch, "
+                         "profiles/fp64_pass_kernels_fermat_batch256.md")
+
+
 def run_ours(args):
     rank, world, local = rank_info()
     dist = None
@@ -195,15 +203,10 @@ def run_ours(args):
     device = local
     import ctypes as C
 
-    # the autotuned four-step shapes of this GPU (shapes only: the FFT lengths stay the ones the
-    # reference's length chooser picks)
-    tuning = os.path.join(ROOT, "ahnum_gb300", "tuning_gb300.txt")
-    if os.path.exists(tuning):
-        with open(tuning) as f:
-            for line in f:
-                parts = line.split()
-                if len(parts) == 4 and not line.startswith("#"):
-                    lib.kc_set_fft_shape(int(parts[0]), int(parts[2]))
+    # the autotuned four-step shapes of this GPU, batched and single-test (shapes only: the FFT
+    # lengths stay the ones the reference's length chooser picks)
+    from ahnum_gb300.tune import load_gb300_tuning
+    load_gb300_tuning(lib)
 
     tests = workload(seed=SEED + rank)
     mean_n = statistics.mean(n for _, n in tests)
@@ -335,7 +338,9 @@ def run_ours(args):
             "clocks": clk.summary(),
             "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12,
                          "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                         "traffic": None, "kernel": names[dom],
+                         "traffic": K_ROWS_DRAM_BYTES if dom == 0 else None,
+                         "traffic_source": K_ROWS_TRAFFIC_SOURCE if dom == 0 else None,
+                         "kernel": names[dom],
                          "peak_source": "measured: DFMA dependent-chain kernel on this GPU "
                                         "(MEASURED_PEAKS.json has no FP64 figure)"},
             "kernels": kernels,

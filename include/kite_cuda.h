@@ -180,8 +180,14 @@ void kc_set_fft_time(uint32_t L, double us);
 int kc_fft_shape_candidates(uint32_t L, uint32_t *R, uint32_t *C, int max);
 /* The shape length L gets now. 0, or -1. */
 int kc_fft_shape(uint32_t L, uint32_t *R, uint32_t *C);
-/* Load a tuning file (shapes and times).  Returns the number of lengths read, -1 if unreadable.
- * The library also loads $KITE_GB300_TUNING, if set, when it plans its first length. */
+/* Shape of one test run alone (latency mode, kc_engine_new with throughput 0) at length L:
+ * R rows and column groups of G in {2, 4, 8} (R = 0: back to the built-in model).  Used for
+ * every number whose digits allow groups of G.  0, or -1 if the shape is unusable. */
+int kc_set_latency_shape(uint32_t L, uint32_t R, int G);
+/* Load a tuning file (shapes and times).  Lines "L us R C G" (five fields) are latency shapes
+ * (kc_set_latency_shape; their times, single-test microseconds, do not steer the length
+ * choice).  Returns the number of lines read, -1 if unreadable.  The library also loads
+ * $KITE_GB300_TUNING, if set, when it plans its first length. */
 int kc_tuning_load(const char *path);
 /* Largest round-off of `squarings` squarings of a seeded residue mod k*2^n-1 at length L on the
  * current GPU (the reference's tools/sweep_err.c measurement); negative on failure. */

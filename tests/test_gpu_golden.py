@@ -71,6 +71,42 @@ def test_large_chain_matches_gmp(lib, c):
         assert g.maxerr() < 0.4
 
 
+def _latency_lines():
+    from ahnum_gb300.tune import LATENCY_FILE
+    with open(LATENCY_FILE) as f:
+        return [tuple(int(float(v)) for v in line.split()) for line in f
+                if not line.startswith("#") and len(line.split()) == 5]
+
+
+TUNED = {c["name"]: c for c in LARGE + CHAINS if c["name"] in ("large_a", "single_49152")}
+
+
+@pytest.mark.parametrize("name", sorted(TUNED))
+def test_shipped_latency_shapes_match_gmp(lib, name):
+    """the single-test shapes shipped in the GB300 tuning file: the engine takes them, and the
+    chain equals GMP's bit for bit"""
+    from ahnum_gb300.kite import Ctx
+    c = TUNED[name]
+    L = LENGTH.get(name, 0) or lib.kc_choose_fft_len(c["k"], c["n"])
+    line = next(t for t in _latency_lines() if t[0] == L)
+    _, _, R, Cc, G = line
+    assert lib.kc_set_latency_shape(L, R, G) == 0
+    try:
+        e = lib.kc_engine_new(c["k"], c["n"], L, None, None, None, 0, 0, 0, 0, -1)
+        assert e
+        r, cc = C.c_uint32(), C.c_uint32()
+        lib.kc_shape(e, C.byref(r), C.byref(cc))
+        assert (r.value, cc.value, lib.kc_group_width(e)) == (R, Cc, G)
+        lib.kc_engine_free(e)
+        with Ctx(c["k"], c["n"], L) as g:
+            x = g.num(_seeded_residue(c["x0_seed"], c["k"], c["n"]))
+            g.square(x, c["squarings"])
+            assert _sha(g.get(x), c["n"]) == c["sha256_limbs"]
+            assert g.maxerr() < 0.4
+    finally:
+        lib.kc_set_latency_shape(L, 0, 0)
+
+
 FERMAT = _load("fermat.json")
 
 

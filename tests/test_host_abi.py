@@ -114,3 +114,25 @@ def test_ctx_new_rejects_cpu_backends(lib):
     o = native.KiteOpts(5, 0, 0, 0)
     assert not lib.kite_ctx_new(9358, 20000, -1, C.byref(o))  # even k
     assert not lib.kite_ctx_new(9357, 20000, 1, C.byref(o))   # c != -1
+
+
+def test_latency_shapes_validated_and_loaded(lib):
+    """the single-test shape overrides refuse shapes the engine cannot run, and the shipped
+    GB300 tuning files load without a GPU"""
+    from ahnum_gb300.tune import LATENCY_FILE, THROUGHPUT_FILE
+    assert lib.kc_set_latency_shape(49152, 96, 3) != 0      # G not in {2, 4, 8}
+    assert lib.kc_set_latency_shape(49152, 100, 2) != 0     # R does not divide H
+    assert lib.kc_set_latency_shape(49152, 2048, 2) != 0    # C = 12: below 16
+    assert lib.kc_set_latency_shape(49152, 96, 2) == 0
+    assert lib.kc_set_latency_shape(49152, 0, 0) == 0       # back to the model
+    assert lib.kc_tuning_load(LATENCY_FILE.encode()) >= 2
+    assert lib.kc_tuning_load(THROUGHPUT_FILE.encode()) >= 10
+    # leave the process as it was: no shapes, no measured times (they steer the length choice)
+    for path in (LATENCY_FILE, THROUGHPUT_FILE):
+        with open(path) as f:
+            for line in f:
+                if not line.startswith("#") and line.split():
+                    L = int(line.split()[0])
+                    lib.kc_set_latency_shape(L, 0, 0)
+                    lib.kc_set_fft_shape(L, 0)
+                    lib.kc_set_fft_time(L, 0.0)
