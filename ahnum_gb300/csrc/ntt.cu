@@ -488,16 +488,40 @@ __global__ void __launch_bounds__(kReduceThreads) kn_reduce(const Desc *descs, c
     {
         const uint32_t nseg = NP >> 3, per = (nseg + T - 1) / T;
         const uint32_t s0 = (uint32_t)t * per, s1 = min(nseg, s0 + per);
+        ulonglong2 *__restrict__ pw2 = reinterpret_cast<ulonglong2 *>(pw);
         u128 acc = 0;
-        for (uint32_t sg = s0; sg < s1; sg++) {
-            if (sg > s0) {
-                const ulonglong2 c = seg[sg - 1];
-                acc += ((u128)c.y << 64) | c.x;
+        // A segment's carry (< 2^(w+20)) almost always settles within the segment's first two
+        // words.  So SB segments at a time, their carries and first two words are loaded
+        // together before the carry walks through them: a thread waits for memory about once
+        // per batch instead of once per word; the rare longer carries continue word by word.
+        constexpr int SB = 4;
+        for (uint32_t sb = s0; sb < s1; sb += SB) {
+            ulonglong2 c[SB], v[SB];
+#pragma unroll
+            for (int q = 0; q < SB; q++) {
+                const uint32_t sg = sb + q;
+                const bool in = sg < s1;
+                c[q] = in && sg > s0 ? seg[sg - 1] : make_ulonglong2(0, 0);
+                v[q] = in ? pw2[sg * 4] : make_ulonglong2(0, 0);
             }
-            for (uint32_t j = sg << 3; acc != 0 && j < (sg << 3) + 8; j++) {
-                acc += pw[j];
-                pw[j] = (uint64_t)acc & M;
+#pragma unroll
+            for (int q = 0; q < SB; q++) {
+                const uint32_t sg = sb + q;
+                if (sg >= s1) break;
+                acc += ((u128)c[q].y << 64) | c[q].x;
+                if (acc == 0) continue;  // words below 2^w: a zero carry leaves them as they are
+                acc += v[q].x;
+                v[q].x = (uint64_t)acc & M;
                 acc >>= w;
+                acc += v[q].y;
+                v[q].y = (uint64_t)acc & M;
+                acc >>= w;
+                pw2[sg * 4] = v[q];
+                for (uint32_t j = (sg << 3) + 2; acc != 0 && j < (sg << 3) + 8; j++) {
+                    acc += pw[j];
+                    pw[j] = (uint64_t)acc & M;
+                    acc >>= w;
+                }
             }
         }
         if (s1 > s0) {
