@@ -80,6 +80,7 @@ struct kc_batch {
         TestDesc *d_desc = nullptr, *h_desc = nullptr;
         WorkItem *d_rows = nullptr, *h_rows = nullptr, *d_cols = nullptr, *h_cols = nullptr;
         int *d_cnt = nullptr, *h_cnt = nullptr;
+        unsigned *d_flow = nullptr;  // control words of the persistent kernel (kernels.h)
     } lists[2];
     unsigned long long *h_err = nullptr;  // pinned, one per slot
     int cap_err = 0;
@@ -88,6 +89,9 @@ struct kc_batch {
     uint32_t graph_B = 0;
     int grid = 0;
     int threads = 128;  // block size of the pass kernels
+    bool persistent = true;       // squaring blocks as persistent k_squarings launches
+    uint32_t steps_per_launch = 100;
+    unsigned *h_flow = nullptr;   // pinned: the timeout word read back after each block
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int err = 0;
     const char *what = "";      // the step that failed, for kc_batch_error_string
@@ -112,6 +116,7 @@ void free_lists(kc_batch::Lists &l) {
     cudaFree(l.d_rows);
     cudaFree(l.d_cols);
     cudaFree(l.d_cnt);
+    cudaFree(l.d_flow);
     if (l.h_desc) cudaFreeHost(l.h_desc);
     if (l.h_rows) cudaFreeHost(l.h_rows);
     if (l.h_cols) cudaFreeHost(l.h_cols);
@@ -129,6 +134,8 @@ bool grow_lists(kc_batch *b, kc_batch::Lists &l, int tests, int rows, int cols) 
            bok(b, cudaMalloc((void **)&l.d_rows, l.cap_rows * sizeof(WorkItem))) &&
            bok(b, cudaMalloc((void **)&l.d_cols, l.cap_cols * sizeof(WorkItem))) &&
            bok(b, cudaMalloc((void **)&l.d_cnt, 2 * sizeof(int))) &&
+           bok(b, cudaMalloc((void **)&l.d_flow, (kFlowDone + l.cap_tests) * sizeof(unsigned))) &&
+           bok(b, cudaMemsetAsync(l.d_flow, 0, (kFlowDone + l.cap_tests) * sizeof(unsigned), b->stream)) &&
            bok(b, cudaMallocHost((void **)&l.h_desc, l.cap_tests * sizeof(TestDesc))) &&
            bok(b, cudaMallocHost((void **)&l.h_rows, l.cap_rows * sizeof(WorkItem))) &&
            bok(b, cudaMallocHost((void **)&l.h_cols, l.cap_cols * sizeof(WorkItem))) &&
@@ -436,13 +443,32 @@ bool ensure_graph(kc_batch *b, const kc_batch::Lists &l, size_t row_lane, size_t
     }
     LaunchSet s = launch_set(b, l, row_lane, col_smem);
     cudaGraph_t g;
+    const int sq_grid = b->persistent ? squarings_grid(s, b->nsm) : 0;
     if (!bok(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal))) return false;
-    for (uint32_t j = 0; j < b->B; j++) {
-        launch_rows(s, false, nullptr, nullptr, (int)j);
-        launch_col_inverse(s, true, nullptr, (int)j);
-        launch_col_forward(s, nullptr, true, (int)j);
+    bool launched = true;
+    if (b->persistent) {
+        // persistent launches of steps_per_launch squarings each; the queue position and the
+        // per-test counters start at zero in every launch, the timeout word is left alone
+        const size_t done_bytes = (size_t)l.cap_tests * sizeof(unsigned);
+        for (uint32_t j = 0; j < b->B && launched; j += b->steps_per_launch) {
+            const uint32_t n = std::min(b->steps_per_launch, b->B - j);
+            launched = bok(b, cudaMemsetAsync(l.d_flow + kFlowNext, 0, sizeof(unsigned), b->stream)) &&
+                       bok(b, cudaMemsetAsync(l.d_flow + kFlowDone, 0, done_bytes, b->stream)) &&
+                       launch_squarings(s, l.d_flow, (int)j, (int)n, sq_grid) == 0;
+        }
+    } else {
+        for (uint32_t j = 0; j < b->B; j++) {
+            launch_rows(s, false, nullptr, nullptr, (int)j);
+            launch_col_inverse(s, true, nullptr, (int)j);
+            launch_col_forward(s, nullptr, true, (int)j);
+        }
     }
     if (!bok(b, cudaStreamEndCapture(b->stream, &g))) return false;
+    if (!launched) {
+        cudaGraphDestroy(g);
+        b->what = "launching the persistent squaring kernel";
+        return false;
+    }
     bool ok = bok(b, cudaGraphInstantiate(&b->graph, g, 0));
     cudaGraphDestroy(g);
     b->graph_B = b->B;
@@ -477,6 +503,13 @@ kc_batch *kc_batch_new(int device, uint32_t gerbicz_block, uint32_t gerbicz_bloc
     b->threads = 128;
     if (const char *t = getenv("KITE_GB300_BATCH_THREADS")) b->threads = atoi(t) == 256 ? 256 : 128;
     b->grid = b->nsm * (kThreads * kMinBlocks / b->threads);
+    // A Gerbicz block's squarings run as persistent launches of k_squarings (steps_per_launch
+    // squarings each) unless KITE_GB300_BATCH_PERSISTENT=0 selects three launches per squaring.
+    if (const char *t = getenv("KITE_GB300_BATCH_PERSISTENT")) b->persistent = atoi(t) != 0;
+    if (const char *t = getenv("KITE_GB300_STEPS_PER_LAUNCH")) {
+        const int v = atoi(t);
+        if (v > 0) b->steps_per_launch = (uint32_t)v;
+    }
     if (!bok(b, cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) || !bok(b, cudaEventCreate(&b->ev0)) ||
         !bok(b, cudaEventCreate(&b->ev1))) {
         kc_batch_free(b);
@@ -494,6 +527,7 @@ void kc_batch_free(kc_batch *b) {
     free_lists(b->lists[0]);
     free_lists(b->lists[1]);
     if (b->h_err) cudaFreeHost(b->h_err);
+    if (b->h_flow) cudaFreeHost(b->h_flow);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -624,7 +658,18 @@ int kc_batch_step(kc_batch *b, uint32_t blocks, double *gpu_ms) {
             b->d2h += 8;
             bok(b, cudaMemsetAsync(s.e->d_maxerr, 0, 8, b->stream));
         }
+        if (b->persistent) {
+            if (!b->h_flow && !bok(b, cudaMallocHost((void **)&b->h_flow, sizeof(unsigned)))) return b->err;
+            bok(b, cudaMemcpyAsync(b->h_flow, b->lists[0].d_flow + kFlowTimeout, sizeof(unsigned),
+                                   cudaMemcpyDeviceToHost, b->stream));
+            b->d2h += sizeof(unsigned);
+        }
         if (!bok(b, cudaStreamSynchronize(b->stream))) return b->err;
+        if (b->persistent && *b->h_flow) {
+            // a CTA gave up waiting for another's item: the block's numbers are not to be trusted
+            b->err = -(int)cudaErrorLaunchTimeout;
+            return fail(b, "a CTA of the persistent squaring kernel timed out waiting for another's item");
+        }
         float ms = 0;
         cudaEventElapsedTime(&ms, b->ev0, b->ev1);
         ms_total += ms;
@@ -822,6 +867,55 @@ int kc_batch_profile(kc_batch *b, uint32_t squarings, double *ms, double *flops)
         if (flops) flops[q] = fl[q];
     }
     return b->err;
+}
+
+int kc_batch_profile_steps(kc_batch *b, uint32_t squarings, double *ms, double *flops) {
+    cudaSetDevice(b->device);
+    if (squarings == 0) return -1;
+    std::vector<Entry> sq;
+    double fl = 0;
+    for (auto &s : b->slots) {
+        if (!s.used || s.phase != Phase::Run) continue;
+        bok(b, cudaMemcpyAsync(s.t, s.x, (size_t)s.e->lay.L * 8, cudaMemcpyDeviceToDevice, b->stream));
+        sq.push_back({&s, s.t, nullptr, 1 << 30, 4, false});
+        const LengthPlan &P = *s.e->plan;
+        const double H = P.H, L = P.L;
+        fl += 10.0 * H * std::log2((double)P.C) + 10.0 * L + 2 * (5.0 * H * std::log2((double)P.R) + 7.0 * L);
+    }
+    if (sq.empty()) return -1;
+    size_t row_lane, col_smem;
+    max_smem(b, row_lane, col_smem);
+    row_lane = std::max(row_lane, b->graph_row_smem);
+    col_smem = std::max(col_smem, b->graph_col_smem);
+    if (kernels_prepare(row_lane * 6, col_smem)) return -1;
+    kc_batch::Lists &l = b->lists[1];
+    if (!fill_lists(b, l, sq)) return b->err ? b->err : -1;
+    LaunchSet s = launch_set(b, l, row_lane, col_smem);
+    const size_t words = (size_t)kFlowDone + l.cap_tests;
+    const int grid = squarings_grid(s, b->nsm);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float t = 0;
+    int rc = 0;
+    for (int rep = 0; rep < 2 && !rc; rep++) {  // the first launch warms up
+        bok(b, cudaMemsetAsync(l.d_flow, 0, words * sizeof(unsigned), b->stream));
+        cudaEventRecord(e0, b->stream);
+        rc = launch_squarings(s, l.d_flow, 0, (int)squarings, grid);
+        cudaEventRecord(e1, b->stream);
+        if (!bok(b, cudaEventSynchronize(e1))) rc = b->err;
+    }
+    if (!rc) cudaEventElapsedTime(&t, e0, e1);
+    unsigned timeout = 0;
+    if (!rc && bok(b, cudaMemcpy(&timeout, l.d_flow + kFlowTimeout, sizeof timeout, cudaMemcpyDeviceToHost)) && timeout)
+        rc = -1;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (auto &sl : b->slots)
+        if (sl.used && sl.phase == Phase::Run) kc_reset_maxerr(sl.e);
+    if (ms) *ms = t;
+    if (flops) *flops = fl * squarings;
+    return rc ? rc : b->err;
 }
 
 double kc_fp64_peak(int device) {

@@ -14,6 +14,7 @@
 // tests with different lengths.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "fft_device.cuh"
@@ -49,71 +50,77 @@ __device__ __forceinline__ void split_pair(double2 &a, double2 &b, double2 w, bo
     b = make_double2(Xr + Yi, Yr - Xi);
 }
 
+// One row pair of one test: forward row transforms, split square or product, inverse row
+// transforms, written back in place.  Ends with a barrier after its last global write.
+template <bool MUL>
+__device__ __forceinline__ void rows_item(const TestDesc &T, int unit, double2 *x, const double2 *y,
+                                          double2 *sm) {
+    // shared memory: A = rows to transform forward, ls lanes interleaved (x row k_r, x row
+    // R-k_r, and for a product the same rows of y); B = the split's output, 2 lanes, already in
+    // the digit-reversed order the inverse transform wants
+    constexpr int ls = MUL ? 4 : 2;
+    const int C = T.C;
+    double2 *A = sm, *B = sm + (size_t)ls * C;
+    const int2 pr = T.pairs[unit];
+    const bool self = pr.x == pr.y;
+    const double2 *xa = x + (size_t)pr.x * C, *xb = x + (size_t)pr.y * C;
+    for (int c = threadIdx.x; c < C; c += blockDim.x) {
+        const int p = __ldg(&T.posc[c]) * ls;
+        A[p + 0] = __ldcg(&xa[c]);
+        A[p + 1] = __ldcg(&xb[c]);
+        if (MUL) {
+            A[p + 2] = __ldcg(&y[(size_t)pr.x * C + c]);
+            A[p + 3] = __ldcg(&y[(size_t)pr.y * C + c]);
+        }
+    }
+    __syncthreads();
+    smem_fft<false>(A, T.rp, T.twr, ls, self ? (MUL ? 3 : 1) : ls);
+    const double2 *swp = T.sw + (size_t)pr.x * C;
+    const double2 zero = make_double2(0, 0);
+    if (!self) {
+        // U_k in row k_r pairs with U_{H-k} in row R-k_r, column C-1-k_c
+        for (int kc = threadIdx.x; kc < C; kc += blockDim.x) {
+            const int kb = C - 1 - kc;
+            double2 a = A[kc * ls], b = A[kb * ls + 1];
+            const double2 ya = MUL ? A[kc * ls + 2] : zero, yb = MUL ? A[kb * ls + 3] : zero;
+            split_pair(a, b, __ldg(&swp[kc]), MUL, ya, yb);
+            B[__ldg(&T.posc[kc]) * 2] = a;
+            B[__ldg(&T.posc[kb]) * 2 + 1] = b;
+        }
+    } else {
+        // rows 0 and R/2 pair with themselves: k_c with (C-k_c) mod C, resp. C-1-k_c
+        for (int kc = threadIdx.x; kc < C; kc += blockDim.x) {
+            const int kb = pr.x == 0 ? (C - kc) % C : C - 1 - kc;
+            if (kb < kc) continue;
+            double2 a = A[kc * ls], b = A[kb * ls];
+            const double2 ya = MUL ? A[kc * ls + 2] : zero, yb = MUL ? A[kb * ls + 2] : zero;
+            split_pair(a, b, __ldg(&swp[kc]), MUL, ya, yb);
+            B[__ldg(&T.posc[kc]) * 2] = a;
+            if (kb != kc) B[__ldg(&T.posc[kb]) * 2] = b;
+        }
+    }
+    __syncthreads();
+    smem_fft<true>(B, T.rp, T.twr, 2, self ? 1 : 2);
+    double2 *oa = x + (size_t)pr.x * C, *ob = x + (size_t)pr.y * C;
+    for (int c = threadIdx.x; c < C; c += blockDim.x) {
+        oa[c] = B[c * 2];
+        if (!self) ob[c] = B[c * 2 + 1];
+    }
+    __syncthreads();
+}
+
 template <bool MUL>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) k_rows(const TestDesc *__restrict__ tests,
                                                    const WorkItem *__restrict__ work, int nwork,
                                                    const int *nwork_dev, int step, double2 *xo,
                                                    const double2 *yo) {
-    // shared memory: A = rows to transform forward, ls lanes interleaved (x row k_r, x row
-    // R-k_r, and for a product the same rows of y); B = the split's output, 2 lanes, already in
-    // the digit-reversed order the inverse transform wants
     extern __shared__ double2 sm[];
-    constexpr int ls = MUL ? 4 : 2;
     if (nwork_dev) nwork = *nwork_dev;
     for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
         const WorkItem it = work[wi];
         const TestDesc &T = tests[it.test];
         if (step >= T.count) continue;
-        double2 *x = xo ? xo : T.x;
-        const double2 *y = MUL ? (yo ? yo : T.y) : nullptr;
-        const int C = T.C;
-        double2 *A = sm, *B = sm + (size_t)ls * C;
-        const int2 pr = T.pairs[it.unit];
-        const bool self = pr.x == pr.y;
-        const double2 *xa = x + (size_t)pr.x * C, *xb = x + (size_t)pr.y * C;
-        for (int c = threadIdx.x; c < C; c += blockDim.x) {
-            const int p = __ldg(&T.posc[c]) * ls;
-            A[p + 0] = xa[c];
-            A[p + 1] = xb[c];
-            if (MUL) {
-                A[p + 2] = y[(size_t)pr.x * C + c];
-                A[p + 3] = y[(size_t)pr.y * C + c];
-            }
-        }
-        __syncthreads();
-        smem_fft<false>(A, T.rp, T.twr, ls, self ? (MUL ? 3 : 1) : ls);
-        const double2 *swp = T.sw + (size_t)pr.x * C;
-        const double2 zero = make_double2(0, 0);
-        if (!self) {
-            // U_k in row k_r pairs with U_{H-k} in row R-k_r, column C-1-k_c
-            for (int kc = threadIdx.x; kc < C; kc += blockDim.x) {
-                const int kb = C - 1 - kc;
-                double2 a = A[kc * ls], b = A[kb * ls + 1];
-                const double2 ya = MUL ? A[kc * ls + 2] : zero, yb = MUL ? A[kb * ls + 3] : zero;
-                split_pair(a, b, __ldg(&swp[kc]), MUL, ya, yb);
-                B[__ldg(&T.posc[kc]) * 2] = a;
-                B[__ldg(&T.posc[kb]) * 2 + 1] = b;
-            }
-        } else {
-            // rows 0 and R/2 pair with themselves: k_c with (C-k_c) mod C, resp. C-1-k_c
-            for (int kc = threadIdx.x; kc < C; kc += blockDim.x) {
-                const int kb = pr.x == 0 ? (C - kc) % C : C - 1 - kc;
-                if (kb < kc) continue;
-                double2 a = A[kc * ls], b = A[kb * ls];
-                const double2 ya = MUL ? A[kc * ls + 2] : zero, yb = MUL ? A[kb * ls + 2] : zero;
-                split_pair(a, b, __ldg(&swp[kc]), MUL, ya, yb);
-                B[__ldg(&T.posc[kc]) * 2] = a;
-                if (kb != kc) B[__ldg(&T.posc[kb]) * 2] = b;
-            }
-        }
-        __syncthreads();
-        smem_fft<true>(B, T.rp, T.twr, 2, self ? 1 : 2);
-        double2 *oa = x + (size_t)pr.x * C, *ob = x + (size_t)pr.y * C;
-        for (int c = threadIdx.x; c < C; c += blockDim.x) {
-            oa[c] = B[c * 2];
-            if (!self) ob[c] = B[c * 2 + 1];
-        }
-        __syncthreads();
+        rows_item<MUL>(T, it.unit, xo ? xo : T.x, MUL ? (yo ? yo : T.y) : nullptr, sm);
     }
 }
 
@@ -186,8 +193,70 @@ __device__ __forceinline__ void load_columns_conj(const TestDesc &T, const doubl
     for (int i = threadIdx.x; i < T.R * G; i += blockDim.x) {
         const int kr = i / G, l = i % G;
         const size_t e = (size_t)kr * C + g * G + l;
-        sm[__ldg(&T.posr[kr]) * G + l] = cmulc(x[e], __ldg(&T.t4[e]));
+        sm[__ldg(&T.posr[kr]) * G + l] = cmulc(__ldcg(&x[e]), __ldg(&T.t4[e]));
     }
+}
+
+// One column group of one test, first half of the column pass: conj twiddle, inverse column
+// transform, unweight and round, round-off, carry within each row segment (carry-out to the
+// next segment's slot), top fold.  Ends with a barrier after its last global write.
+template <bool ERR, int G>
+__device__ __forceinline__ void col_inverse_item(const TestDesc &T, int g, int step, const double2 *x,
+                                                 double2 *sm) {
+    long long *smd = reinterpret_cast<long long *>(sm);
+    const bool track = ERR && (step % T.err_every == 0);
+    const int R = T.R, C = T.C;
+    load_columns_conj<G>(T, x, g, sm);
+    __syncthreads();
+    smem_fft<true>(sm, T.cp, T.twc, G, G);
+    // unweight, scale and round every value in parallel: one FMA with the magic constant
+    // (two more when the round-off is tracked); the integer is read from the encoding
+    unsigned long long emax = 0;
+    for (int i = threadIdx.x; i < R * G; i += blockDim.x) {
+        const int r = i / G, l = i % G;
+        const int j = 2 * (r * C + g * G + l);
+        const double2 z = sm[i];
+        const double o0 = __ldg(&T.osc[j]), o1 = __ldg(&T.osc[j + 1]);
+        const double t0 = fma(z.x, o0, kMagic), t1 = fma(z.y, o1, kMagic);
+        const long long b0 = __double_as_longlong(t0), b1 = __double_as_longlong(t1);
+        if (((b0 >> 52) != 0x433) | ((b1 >> 52) != 0x433)) {
+            emax = 0x3FE0000000000000ull;  // |v| >= 2^51: report 0.5, the transform is too short
+        } else if (track) {
+            const unsigned long long e0 = __double_as_longlong(fabs(fma(z.x, o0, kMagic - t0)));
+            const unsigned long long e1 = __double_as_longlong(fabs(fma(z.y, o1, kMagic - t1)));
+            emax = max(emax, max(e0, e1));
+        }
+        smd[2 * i] = b0 - kMagicBits;
+        smd[2 * i + 1] = b1 - kMagicBits;
+    }
+    __syncthreads();
+    // balanced carry along each row segment (16 digits), constants added first; the carry-out
+    // goes to the next segment's slot, the last segment's into the top fold
+    for (int r = threadIdx.x; r < R; r += blockDim.x) {
+        const int j0 = 2 * (r * C + g * G);
+        long long d[2 * G];
+        long long cy = 0;
+#pragma unroll
+        for (int i = 0; i < 2 * G; i++) {
+            long long v = smd[2 * G * r + i];
+            for (int a = 0; a < T.nadd; a++)
+                if (T.addj[a] == j0 + i) v += T.addv[a];
+            v += cy;
+            const int b = __ldg(&T.bits[j0 + i]);
+            const long long q = (v + (1ll << (b - 1))) >> b;
+            d[i] = v - (q << b);
+            cy = q;
+        }
+#pragma unroll
+        for (int i = 0; i < 2 * G; i++) T.dig[j0 + i] = d[i];
+        if (g == T.NG - 1 && r == R - 1) {
+            T.slot[0] = fold_top(T, T.dig, cy);  // this thread's own digits: visible
+        } else {
+            T.slot[g < T.NG - 1 ? (g + 1) * R + r : r + 1] = cy;
+        }
+    }
+    block_max_err(emax, T.maxerr);  // every thread of the block reaches this
+    __syncthreads();
 }
 
 template <bool ERR, int G>
@@ -196,67 +265,54 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_inverse(const Test
                                                           int nwork, const int *nwork_dev,
                                                           int step, const double2 *xo) {
     extern __shared__ double2 sm[];
-    long long *smd = reinterpret_cast<long long *>(sm);
     if (nwork_dev) nwork = *nwork_dev;
     for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
         const WorkItem it = work[wi];
         const TestDesc &T = tests[it.test];
         if (step >= T.count) continue;
-        const bool track = ERR && (step % T.err_every == 0);
-        const double2 *x = xo ? xo : T.x;
-        const int R = T.R, C = T.C, g = it.unit;
-        load_columns_conj<G>(T, x, g, sm);
-        __syncthreads();
-        smem_fft<true>(sm, T.cp, T.twc, G, G);
-        // unweight, scale and round every value in parallel: one FMA with the magic constant
-        // (two more when the round-off is tracked); the integer is read from the encoding
-        unsigned long long emax = 0;
-        for (int i = threadIdx.x; i < R * G; i += blockDim.x) {
-            const int r = i / G, l = i % G;
-            const int j = 2 * (r * C + g * G + l);
-            const double2 z = sm[i];
-            const double o0 = __ldg(&T.osc[j]), o1 = __ldg(&T.osc[j + 1]);
-            const double t0 = fma(z.x, o0, kMagic), t1 = fma(z.y, o1, kMagic);
-            const long long b0 = __double_as_longlong(t0), b1 = __double_as_longlong(t1);
-            if (((b0 >> 52) != 0x433) | ((b1 >> 52) != 0x433)) {
-                emax = 0x3FE0000000000000ull;  // |v| >= 2^51: report 0.5, the transform is too short
-            } else if (track) {
-                const unsigned long long e0 = __double_as_longlong(fabs(fma(z.x, o0, kMagic - t0)));
-                const unsigned long long e1 = __double_as_longlong(fabs(fma(z.y, o1, kMagic - t1)));
-                emax = max(emax, max(e0, e1));
-            }
-            smd[2 * i] = b0 - kMagicBits;
-            smd[2 * i + 1] = b1 - kMagicBits;
-        }
-        __syncthreads();
-        // balanced carry along each row segment (16 digits), constants added first; the carry-out
-        // goes to the next segment's slot, the last segment's into the top fold
-        for (int r = threadIdx.x; r < R; r += blockDim.x) {
-            const int j0 = 2 * (r * C + g * G);
-            long long d[2 * G];
-            long long cy = 0;
+        col_inverse_item<ERR, G>(T, it.unit, step, xo ? xo : T.x, sm);
+    }
+}
+
+// One column group of one test, second half of the column pass: absorb the carry-in,
+// reweight, forward column transform, twiddle.  Ends with a barrier after its last global write.
+template <int G>
+__device__ __forceinline__ void col_forward_item(const TestDesc &T, int g, double2 *x, bool use_slots,
+                                                 double2 *sm) {
+    const int R = T.R, C = T.C;
+    // absorb the carry-in into the segment's first digits (the last digit takes any rest),
+    // reweight, and place the row at its digit-reversed position
+    for (int r = threadIdx.x; r < R; r += blockDim.x) {
+        const int j0 = 2 * (r * C + g * G);
+        long long d[2 * G];
 #pragma unroll
-            for (int i = 0; i < 2 * G; i++) {
-                long long v = smd[2 * G * r + i];
-                for (int a = 0; a < T.nadd; a++)
-                    if (T.addj[a] == j0 + i) v += T.addv[a];
-                v += cy;
+        for (int i = 0; i < 2 * G; i++) d[i] = __ldcg(&T.dig[j0 + i]);
+        long long cy = use_slots ? __ldcg(&T.slot[g * R + r]) : 0;
+#pragma unroll
+        for (int i = 0; i < 2 * G - 1; i++) {
+            if (cy) {
                 const int b = __ldg(&T.bits[j0 + i]);
+                const long long v = d[i] + cy;
                 const long long q = (v + (1ll << (b - 1))) >> b;
                 d[i] = v - (q << b);
                 cy = q;
             }
-#pragma unroll
-            for (int i = 0; i < 2 * G; i++) T.dig[j0 + i] = d[i];
-            if (g == T.NG - 1 && r == R - 1) {
-                T.slot[0] = fold_top(T, T.dig, cy);  // this thread's own digits: visible
-            } else {
-                T.slot[g < T.NG - 1 ? (g + 1) * R + r : r + 1] = cy;
-            }
         }
-        block_max_err(emax, T.maxerr);  // every thread of the block reaches this
-        __syncthreads();
+        d[2 * G - 1] += cy;
+        double2 *row = sm + __ldg(&T.posr[r]) * G;
+#pragma unroll
+        for (int l = 0; l < G; l++)
+            row[l] = make_double2((double)d[2 * l] * __ldg(&T.w[j0 + 2 * l]),
+                                  (double)d[2 * l + 1] * __ldg(&T.w[j0 + 2 * l + 1]));
     }
+    __syncthreads();
+    smem_fft<false>(sm, T.cp, T.twc, G, G);
+    for (int i = threadIdx.x; i < R * G; i += blockDim.x) {
+        const int kr = i / G, l = i % G;
+        const size_t e = (size_t)kr * C + g * G + l;
+        x[e] = cmul(sm[i], __ldg(&T.t4[e]));
+    }
+    __syncthreads();
 }
 
 template <int G>
@@ -270,41 +326,90 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_forward(const Test
         const WorkItem it = work[wi];
         const TestDesc &T = tests[it.test];
         if (step >= T.count) continue;
-        double2 *x = xo ? xo : T.x;
-        const int R = T.R, C = T.C, g = it.unit;
-        // absorb the carry-in into the segment's first digits (the last digit takes any rest),
-        // reweight, and place the row at its digit-reversed position
-        for (int r = threadIdx.x; r < R; r += blockDim.x) {
-            const int j0 = 2 * (r * C + g * G);
-            long long d[2 * G];
-#pragma unroll
-            for (int i = 0; i < 2 * G; i++) d[i] = T.dig[j0 + i];
-            long long cy = use_slots ? T.slot[g * R + r] : 0;
-#pragma unroll
-            for (int i = 0; i < 2 * G - 1; i++) {
-                if (cy) {
-                    const int b = __ldg(&T.bits[j0 + i]);
-                    const long long v = d[i] + cy;
-                    const long long q = (v + (1ll << (b - 1))) >> b;
-                    d[i] = v - (q << b);
-                    cy = q;
-                }
+        col_forward_item<G>(T, it.unit, xo ? xo : T.x, use_slots != 0, sm);
+    }
+}
+
+// Waits until *ctr >= need, reading it with acquire semantics at GPU scope.  Gives up (returns
+// false) when another CTA has raised *flag, or after about two seconds, raising *flag itself.
+__device__ __noinline__ bool wait_count(const unsigned *ctr, unsigned need, unsigned *flag) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
+    if (v >= need) return true;
+    const long long t0 = clock64();
+    for (;;) {
+        __nanosleep(128);
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
+        if (v >= need) return true;
+        if (*(volatile const unsigned *)flag) return false;
+        if (clock64() - t0 > kWaitCycles) {
+            atomicOr(flag, 1u);
+            return false;
+        }
+    }
+}
+
+// `nsteps` squarings of every test of the work lists in one persistent launch.
+//
+// The work is one queue, taken in order by atomically incrementing flow[kFlowNext]: for each
+// step, every row pair, then every column group (inverse half), then every column group
+// (forward half).  A CTA that takes an item first waits until the test's previous phase is
+// complete: flow[kFlowDone + test] counts the test's finished items, and the phases of one test
+// follow each other, so item counts alone say which phase is done.  Different tests overlap
+// freely, so no CTA idles at the end of a phase or of a step, as it would at the end of a
+// kernel launch.  Every wait is on items earlier in the queue, which CTAs already running hold,
+// so each wait ends; one that runs out of time raises flow[kFlowTimeout] and every CTA returns.
+template <int G>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_squarings(const TestDesc *__restrict__ tests,
+                                                        const WorkItem *__restrict__ rows, int nrows,
+                                                        const int *nrows_dev,
+                                                        const WorkItem *__restrict__ cols, int ncols,
+                                                        const int *ncols_dev, int step0, int nsteps,
+                                                        unsigned *flow) {
+    extern __shared__ double2 sm[];
+    __shared__ unsigned s_q;
+    __shared__ int s_ok;
+    const unsigned nr = (unsigned)(nrows_dev ? *nrows_dev : nrows);
+    const unsigned nc = (unsigned)(ncols_dev ? *ncols_dev : ncols);
+    const unsigned per_step = nr + 2 * nc;
+    const unsigned total = per_step * (unsigned)nsteps;
+    for (;;) {
+        __syncthreads();  // every thread has read the previous item's s_q
+        if (threadIdx.x == 0) {
+            const unsigned q = atomicAdd(&flow[kFlowNext], 1u);
+            int ok = 1;
+            if (q < total) {
+                const unsigned st = q / per_step, r = q % per_step;
+                const WorkItem it = r < nr ? rows[r] : cols[(r - nr) % nc];
+                const TestDesc &T = tests[it.test];
+                unsigned need = st * (unsigned)(T.npairs + 2 * T.NG);
+                if (r >= nr) need += (unsigned)T.npairs;
+                if (r >= nr + nc) need += (unsigned)T.NG;
+                ok = wait_count(&flow[kFlowDone + it.test], need, &flow[kFlowTimeout]);
             }
-            d[2 * G - 1] += cy;
-            double2 *row = sm + __ldg(&T.posr[r]) * G;
-#pragma unroll
-            for (int l = 0; l < G; l++)
-                row[l] = make_double2((double)d[2 * l] * __ldg(&T.w[j0 + 2 * l]),
-                                      (double)d[2 * l + 1] * __ldg(&T.w[j0 + 2 * l + 1]));
+            s_q = q;
+            s_ok = ok;
         }
         __syncthreads();
-        smem_fft<false>(sm, T.cp, T.twc, G, G);
-        for (int i = threadIdx.x; i < R * G; i += blockDim.x) {
-            const int kr = i / G, l = i % G;
-            const size_t e = (size_t)kr * C + g * G + l;
-            x[e] = cmul(sm[i], __ldg(&T.t4[e]));
+        const unsigned q = s_q;
+        if (q >= total || !s_ok) return;
+        const unsigned st = q / per_step, r = q % per_step;
+        const WorkItem it = r < nr ? rows[r] : cols[(r - nr) % nc];
+        const TestDesc &T = tests[it.test];
+        const int step = step0 + (int)st;
+        if (step < T.count) {
+            if (r < nr)
+                rows_item<false>(T, it.unit, T.x, nullptr, sm);
+            else if (r < nr + nc)
+                col_inverse_item<true, G>(T, it.unit, step, T.x, sm);
+            else
+                col_forward_item<G>(T, it.unit, T.x, true, sm);
         }
-        __syncthreads();
+        // each item ends with a barrier after its last global write: publish them, then count
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(&flow[kFlowDone + it.test], 1u);
+        }
     }
 }
 
@@ -357,7 +462,7 @@ static int set_smem(const void *fn, size_t bytes) {
 // launches (or captured graphs) of a longer length fail.
 int kernels_prepare(size_t row_smem, size_t col_smem) {
     static std::mutex mu;
-    static size_t row_hw[kMaxDevices] = {}, col_hw[kMaxDevices] = {};
+    static size_t row_hw[kMaxDevices] = {}, col_hw[kMaxDevices] = {}, sq_hw[kMaxDevices] = {};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return -1;
     std::lock_guard<std::mutex> lock(mu);
@@ -381,6 +486,14 @@ int kernels_prepare(size_t row_smem, size_t col_smem) {
         rc |= set_smem((const void *)k_col_digits<4>, col_smem);
         rc |= set_smem((const void *)k_col_digits<8>, col_smem);
         if (!rc) col_hw[dev] = col_smem;
+    }
+    const size_t sq_smem = squarings_smem(row_smem, col_smem);
+    if (sq_smem > sq_hw[dev]) {
+        int r2 = set_smem((const void *)k_squarings<2>, sq_smem);
+        r2 |= set_smem((const void *)k_squarings<4>, sq_smem);
+        r2 |= set_smem((const void *)k_squarings<8>, sq_smem);
+        if (!r2) sq_hw[dev] = sq_smem;
+        rc |= r2;
     }
     return rc;
 }
@@ -416,6 +529,40 @@ void launch_col_forward(const LaunchSet &s, double2 *x, bool use_slots, int step
     case 4: k_col_forward<4><<<s.grid_cols, s.threads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x, u); break;
     default: k_col_forward<8><<<s.grid_cols, s.threads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x, u); break;
     }
+}
+
+// shared memory of k_squarings: a row pair squared (4 lanes of the longest row; row_smem is
+// sized for the 6 lanes of a product) or a column group
+size_t squarings_smem(size_t row_smem, size_t col_smem) { return std::max(row_smem / 6 * 4, col_smem); }
+
+template <int G>
+static int squarings_per_sm(const LaunchSet &s) {
+    int per_sm = 0;
+    const size_t smem = squarings_smem(s.row_smem_per_lane * 6, s.col_smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_squarings<G>, s.threads, smem) != cudaSuccess)
+        return 0;
+    return per_sm;
+}
+
+int squarings_grid(const LaunchSet &s, int nsm) {
+    switch (s.G) {
+    case 2: return squarings_per_sm<2>(s) * nsm;
+    case 4: return squarings_per_sm<4>(s) * nsm;
+    default: return squarings_per_sm<8>(s) * nsm;
+    }
+}
+
+int launch_squarings(const LaunchSet &s, unsigned *flow, int step0, int nsteps, int grid) {
+    if (grid < 1) return -1;
+    const size_t smem = squarings_smem(s.row_smem_per_lane * 6, s.col_smem);
+#define KG_SQ_ARGS s.tests, s.rows, s.nrows, s.nrows_dev, s.cols, s.ncols, s.ncols_dev, step0, nsteps, flow
+    switch (s.G) {
+    case 2: k_squarings<2><<<grid, s.threads, smem, s.stream>>>(KG_SQ_ARGS); break;
+    case 4: k_squarings<4><<<grid, s.threads, smem, s.stream>>>(KG_SQ_ARGS); break;
+    default: k_squarings<8><<<grid, s.threads, smem, s.stream>>>(KG_SQ_ARGS); break;
+    }
+#undef KG_SQ_ARGS
+    return 0;
 }
 
 void launch_col_digits(const LaunchSet &s, const double2 *x) {

@@ -11,6 +11,15 @@ constexpr int kThreads = 256;
 constexpr int kMinBlocks = 4;   // CTAs per SM the pass kernels are compiled for (64 registers)
 constexpr int kMaxDevices = 64;  // devices tracked by the per-device tables of this library
 
+// Control words of the persistent squaring kernel (device memory, zeroed before each launch):
+// flow[kFlowNext] the next queue position, flow[kFlowTimeout] non-zero when a wait gave up,
+// flow[kFlowDone + t] the items of test t finished in this launch.
+constexpr int kFlowNext = 0;
+constexpr int kFlowTimeout = 1;
+constexpr int kFlowDone = 32;
+// cycles a CTA of k_squarings waits for another CTA's item before it gives up (about 2 s)
+constexpr long long kWaitCycles = 4000000000ll;
+
 // Everything one launch of the pass kernels needs: the test table, the work lists and the
 // grid sizes.  The same set serves a single test and a batch.
 struct LaunchSet {
@@ -42,6 +51,14 @@ void launch_col_forward(const LaunchSet &s, double2 *x, bool use_slots, int step
 // the result is written to out[0] only if the chains overflow (never).
 void launch_fp64_probe(cudaStream_t st, int grid, int block, int iters, double *out);
 void launch_col_digits(const LaunchSet &s, const double2 *x);
+// Squarings step0 .. step0+nsteps-1 of every test of the lists in one persistent launch
+// (k_squarings) of `grid` CTAs.  `flow` holds kFlowDone + (tests) words, zeroed before the
+// launch.  Returns -1 if grid < 1.
+int launch_squarings(const LaunchSet &s, unsigned *flow, int step0, int nsteps, int grid);
+// CTAs of k_squarings that fit at once on nsm SMs for this set (0 if none); call it outside
+// stream capture.
+int squarings_grid(const LaunchSet &s, int nsm);
+size_t squarings_smem(size_t row_smem, size_t col_smem);
 // op: 0 copy, 1 add, 2 sub
 void launch_elementwise(cudaStream_t st, double2 *x, const double2 *y, size_t n, int op);
 

@@ -7,7 +7,8 @@ the FFT length the reference's length chooser picks (16K-56K words).  Synthetic,
 reference publishes no benchmark suite.
 
 A step is one Gerbicz block of every test: B = 1000 squarings of each test's x (one CUDA graph
-of 3000 kernels over all 256 tests) plus the block's product d <- d*x.  The check of every M = 250
+of ten persistent launches of 100 squarings each over all 256 tests) plus the block's product
+d <- d*x.  The check of every M = 250
 blocks (another B squarings and a product) is charged analytically, as a factor (1 + 1/M).
 Throughput is the steady state of a served batch whose slots are refilled with tests of the same
 distribution:  tests/hour = 3600 * slots * B / (T_block * (1 + 1/M) * mean(n)).
@@ -16,8 +17,8 @@ distribution:  tests/hour = 3600 * slots * B / (T_block * (1 + 1/M) * mean(n)).
   e2e       the same through the C ABI with host buffers: wall-clock kc_batch_step calls (their
             H2D slot tables and work lists, D2H round-off), plus per-test admission (H2D of
             x0 and the tables) and read-back (D2H of the residue), amortised per test
-  roofline  the dominant kernel's algorithmic FP64 FLOPs per launch over its CUDA-event time,
-            against the FP64 FMA peak measured on this GPU by a DFMA kernel
+  roofline  the persistent squaring kernel's algorithmic FP64 FLOPs per launch over its
+            CUDA-event time, against the FP64 FMA peak measured on this GPU by a DFMA kernel
   cpu_baseline  the reference's arithmetic on the host: the CPU oracle's port of the
             reference's `ref` backend (one test per core on all cores) over a bounded sample
 
@@ -180,12 +181,16 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-# DRAM bytes (read + write) of one k_rows launch over this workload's 256 tests, from an ncu
-# capture of the same launch: ncu --set full --clock-control none -k regex:k_rows -s 2 -c 1
-# python bench.py --quick --steps 1 --warmup 1 --no-ntt (76.47 MB read + 19.67 MB written)
-K_ROWS_DRAM_BYTES = 96.14e6
-K_ROWS_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_rows launch, "
-                         "profiles/fp64_pass_kernels_fermat_batch256.md")
+# squarings of every test per persistent launch (the batch's default, KITE_GB300_STEPS_PER_LAUNCH)
+STEPS_PER_LAUNCH = 100
+# DRAM bytes (read + write) of one k_squarings launch (100 squarings of this workload's 256
+# tests), from an ncu capture of the same launch: ncu --metrics
+# gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum --clock-control none
+# -k regex:k_squarings -s 2 -c 1 python bench.py --quick --steps 1 --warmup 1 --no-ntt
+# (35.01 GB read + 20.61 GB written)
+K_SQ_DRAM_BYTES = 55.62e9
+K_SQ_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_squarings launch, "
+                       "profiles/k_squarings_fermat_batch256.md")
 
 
 def run_ours(args):
@@ -263,18 +268,24 @@ def run_ours(args):
     e2e_per_test = (t_admit + t_read) / SLOTS + mean_n * ovh * t_block_wall / (SLOTS * BLOCK)
     e2e_value = 3600.0 / e2e_per_test * world
 
-    # ---- roofline of the dominant kernel (after the timed region, on the same stream)
+    # ---- roofline (after the timed region, on the same stream): the persistent kernel the
+    #      block runs, and each pass as a kernel of its own for the split of the time
+    msp, flp = C.c_double(), C.c_double()
+    if lib.kc_batch_profile_steps(b.h, STEPS_PER_LAUNCH, C.byref(msp), C.byref(flp)) != 0:
+        raise RuntimeError("kc_batch_profile_steps failed")
     ms3 = (C.c_double * 3)()
     fl3 = (C.c_double * 3)()
-    rc = lib.kc_batch_profile(b.h, 5, ms3, fl3)
+    lib.kc_batch_profile(b.h, 5, ms3, fl3)
     peak = lib.kc_fp64_peak(device)
-    names = ["k_rows (row FFT + split square)", "k_col_inverse (inverse column FFT + round + carry)",
-             "k_col_forward (carry-in + forward column FFT)"]
-    dom = max(range(3), key=lambda q: ms3[q])
-    achieved = fl3[dom] / (ms3[dom] * 1e-3) if ms3[dom] > 0 else 0.0
-    kernels = {names[q]: {"ms_per_launch": ms3[q], "gflop_per_launch": fl3[q] / 1e9,
-                          "tflops": fl3[q] / (ms3[q] * 1e-3) / 1e12 if ms3[q] else 0}
-               for q in range(3)}
+    sq_name = f"k_squarings (persistent: {STEPS_PER_LAUNCH} squarings of every test per launch)"
+    achieved = flp.value / (msp.value * 1e-3) if msp.value > 0 else 0.0
+    names = ["k_rows (row FFT + split square), alone", "k_col_inverse (inverse column FFT + round + carry), alone",
+             "k_col_forward (carry-in + forward column FFT), alone"]
+    kernels = {sq_name: {"ms_per_launch": msp.value, "gflop_per_launch": flp.value / 1e9,
+                         "tflops": achieved / 1e12}}
+    kernels.update({names[q]: {"ms_per_launch": ms3[q], "gflop_per_launch": fl3[q] / 1e9,
+                               "tflops": fl3[q] / (ms3[q] * 1e-3) / 1e12 if ms3[q] else 0}
+                    for q in range(3)})
     b.close()
 
     ntt = ntt_leg(lib, tests, mean_n, device) if args.ntt else None
@@ -334,13 +345,12 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": "tests/hour", "h2d_bytes_per_step": h2d.value,
                     "d2h_bytes_per_step": d2h.value,
                     "admission_s": t_admit, "readback_s": t_read, "block_wall_s": t_block_wall},
-            "gpu_launches": args.steps * (3 * BLOCK + 3),
+            "gpu_launches": args.steps * (math.ceil(BLOCK / STEPS_PER_LAUNCH) + 3),
             "clocks": clk.summary(),
             "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12,
                          "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                         "traffic": K_ROWS_DRAM_BYTES if dom == 0 else None,
-                         "traffic_source": K_ROWS_TRAFFIC_SOURCE if dom == 0 else None,
-                         "kernel": names[dom],
+                         "traffic": K_SQ_DRAM_BYTES, "traffic_source": K_SQ_TRAFFIC_SOURCE,
+                         "kernel": sq_name,
                          "peak_source": "measured: DFMA dependent-chain kernel on this GPU "
                                         "(MEASURED_PEAKS.json has no FP64 figure)"},
             "kernels": kernels,

@@ -161,6 +161,12 @@ const char *kc_batch_error_string(const kc_batch *b);
  * F(L) = 5 L log2(L/2) + 24 L split as 10 H log2 C + 10 L, 5 H log2 R + 7 L, 5 H log2 R + 7 L).
  * Only valid while no slot is in its check or tail (it uses t).  0 or a negative CUDA error. */
 int kc_batch_profile(kc_batch *b, uint32_t squarings, double *ms, double *flops);
+/* The same measurement for the form kc_batch_step runs: one persistent launch (k_squarings) of
+ * `squarings` squarings of every running Fermat slot's copy t, after one warm-up launch, timed
+ * with CUDA events on the batch stream.  *ms receives the launch's duration and *flops its
+ * algorithmic FP64 operations (F(L) per slot per squaring).  Same preconditions; 0, -1 if a
+ * wait inside the kernel timed out, or a negative CUDA error. */
+int kc_batch_profile_steps(kc_batch *b, uint32_t squarings, double *ms, double *flops);
 
 /* Measured FP64 FMA throughput of `device` in FLOP/s (2 per FMA), from a dependent-chain DFMA
  * kernel timed with CUDA events: the roofline denominator of this FP64-bound path. */
