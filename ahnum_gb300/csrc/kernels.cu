@@ -186,6 +186,39 @@ __device__ __forceinline__ void block_max_err(unsigned long long v, unsigned lon
 constexpr double kMagic = 6755399441055744.0;
 constexpr long long kMagicBits = 0x4338000000000000ll;
 
+// The 2G digit widths of the row segment starting at word j0, packed four to a word, in one
+// aligned load: j0 is a multiple of 2G (C is a multiple of G), and the table starts on a
+// 256-byte boundary.  seg_width(w, i) unpacks width i.
+template <int G>
+struct SegWidths {
+    unsigned w[2 * G / 4];
+};
+
+template <int G>
+__device__ __forceinline__ SegWidths<G> load_segment_widths(const uint8_t *bits, int j0) {
+    static_assert(G == 2 || G == 4 || G == 8, "column groups of 2, 4 or 8");
+    SegWidths<G> s;
+    if constexpr (G == 8) {
+        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(bits + j0));
+        s.w[0] = v.x;
+        s.w[1] = v.y;
+        s.w[2] = v.z;
+        s.w[3] = v.w;
+    } else if constexpr (G == 4) {
+        const uint2 v = __ldg(reinterpret_cast<const uint2 *>(bits + j0));
+        s.w[0] = v.x;
+        s.w[1] = v.y;
+    } else {
+        s.w[0] = __ldg(reinterpret_cast<const unsigned *>(bits + j0));
+    }
+    return s;
+}
+
+template <int G>
+__device__ __forceinline__ int seg_width(const SegWidths<G> &s, int i) {
+    return (int)((s.w[i / 4] >> (8 * (i % 4))) & 0xffu);
+}
+
 // load the group's columns times conj(w_H^{c k_r}) into digit-reversed rows of the buffer
 template <int G>
 __device__ __forceinline__ void load_columns_conj(const TestDesc &T, const double2 *x, int g, double2 *sm) {
@@ -216,7 +249,8 @@ __device__ __forceinline__ void col_inverse_item(const TestDesc &T, int g, int s
         const int r = i / G, l = i % G;
         const int j = 2 * (r * C + g * G + l);
         const double2 z = sm[i];
-        const double o0 = __ldg(&T.osc[j]), o1 = __ldg(&T.osc[j + 1]);
+        const double2 o = __ldg(reinterpret_cast<const double2 *>(T.osc + j));  // j is even
+        const double o0 = o.x, o1 = o.y;
         const double t0 = fma(z.x, o0, kMagic), t1 = fma(z.y, o1, kMagic);
         const long long b0 = __double_as_longlong(t0), b1 = __double_as_longlong(t1);
         if (((b0 >> 52) != 0x433) | ((b1 >> 52) != 0x433)) {
@@ -226,8 +260,7 @@ __device__ __forceinline__ void col_inverse_item(const TestDesc &T, int g, int s
             const unsigned long long e1 = __double_as_longlong(fabs(fma(z.y, o1, kMagic - t1)));
             emax = max(emax, max(e0, e1));
         }
-        smd[2 * i] = b0 - kMagicBits;
-        smd[2 * i + 1] = b1 - kMagicBits;
+        reinterpret_cast<longlong2 *>(smd)[i] = make_longlong2(b0 - kMagicBits, b1 - kMagicBits);
     }
     __syncthreads();
     // balanced carry along each row segment (16 digits), constants added first; the carry-out
@@ -235,20 +268,29 @@ __device__ __forceinline__ void col_inverse_item(const TestDesc &T, int g, int s
     for (int r = threadIdx.x; r < R; r += blockDim.x) {
         const int j0 = 2 * (r * C + g * G);
         long long d[2 * G];
+        const SegWidths<G> bw = load_segment_widths<G>(T.bits, j0);
+        const longlong2 *row = reinterpret_cast<const longlong2 *>(smd) + G * r;
+#pragma unroll
+        for (int l = 0; l < G; l++) {
+            const longlong2 p = row[l];
+            d[2 * l] = p.x;
+            d[2 * l + 1] = p.y;
+        }
         long long cy = 0;
 #pragma unroll
         for (int i = 0; i < 2 * G; i++) {
-            long long v = smd[2 * G * r + i];
+            long long v = d[i];
             for (int a = 0; a < T.nadd; a++)
                 if (T.addj[a] == j0 + i) v += T.addv[a];
             v += cy;
-            const int b = __ldg(&T.bits[j0 + i]);
+            const int b = seg_width(bw, i);
             const long long q = (v + (1ll << (b - 1))) >> b;
             d[i] = v - (q << b);
             cy = q;
         }
+        longlong2 *dst = reinterpret_cast<longlong2 *>(T.dig + j0);  // j0 is even
 #pragma unroll
-        for (int i = 0; i < 2 * G; i++) T.dig[j0 + i] = d[i];
+        for (int l = 0; l < G; l++) dst[l] = make_longlong2(d[2 * l], d[2 * l + 1]);
         if (g == T.NG - 1 && r == R - 1) {
             T.slot[0] = fold_top(T, T.dig, cy);  // this thread's own digits: visible
         } else {
@@ -285,13 +327,19 @@ __device__ __forceinline__ void col_forward_item(const TestDesc &T, int g, doubl
     for (int r = threadIdx.x; r < R; r += blockDim.x) {
         const int j0 = 2 * (r * C + g * G);
         long long d[2 * G];
+        const longlong2 *src = reinterpret_cast<const longlong2 *>(T.dig + j0);  // j0 is even
 #pragma unroll
-        for (int i = 0; i < 2 * G; i++) d[i] = __ldcg(&T.dig[j0 + i]);
+        for (int l = 0; l < G; l++) {
+            const longlong2 p = __ldcg(src + l);
+            d[2 * l] = p.x;
+            d[2 * l + 1] = p.y;
+        }
         long long cy = use_slots ? __ldcg(&T.slot[g * R + r]) : 0;
+        const SegWidths<G> bw = load_segment_widths<G>(T.bits, j0);
 #pragma unroll
         for (int i = 0; i < 2 * G - 1; i++) {
             if (cy) {
-                const int b = __ldg(&T.bits[j0 + i]);
+                const int b = seg_width(bw, i);
                 const long long v = d[i] + cy;
                 const long long q = (v + (1ll << (b - 1))) >> b;
                 d[i] = v - (q << b);
@@ -300,10 +348,12 @@ __device__ __forceinline__ void col_forward_item(const TestDesc &T, int g, doubl
         }
         d[2 * G - 1] += cy;
         double2 *row = sm + __ldg(&T.posr[r]) * G;
+        const double2 *wv = reinterpret_cast<const double2 *>(T.w + j0);
 #pragma unroll
-        for (int l = 0; l < G; l++)
-            row[l] = make_double2((double)d[2 * l] * __ldg(&T.w[j0 + 2 * l]),
-                                  (double)d[2 * l + 1] * __ldg(&T.w[j0 + 2 * l + 1]));
+        for (int l = 0; l < G; l++) {
+            const double2 wl = __ldg(wv + l);
+            row[l] = make_double2((double)d[2 * l] * wl.x, (double)d[2 * l + 1] * wl.y);
+        }
     }
     __syncthreads();
     smem_fft<false>(sm, T.cp, T.twc, G, G);
