@@ -448,4 +448,32 @@ void kc_shape(const kc_engine *e, uint32_t *R, uint32_t *C) {
 
 int kc_group_width(const kc_engine *e) { return e->G; }
 
+int kc_engine_wait_selftest(kc_engine *e, uint64_t wait_cycles) {
+    DeviceGuard dg(e->device);
+    int nsm = 0;
+    if (!ok(e, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, e->device))) return e->err;
+    // the engine's column items without its row items: every column item waits for row items
+    // that are not in the queue, so every wait runs out
+    LaunchSet s = e->ls;
+    s.nrows = 0;
+    s.nrows_dev = nullptr;
+    s.ncols_dev = nullptr;
+    const int grid = squarings_grid(s, nsm);
+    const size_t bytes = (kFlowDone + 1) * sizeof(unsigned);
+    unsigned *flow = nullptr;
+    if (!ok(e, cudaMalloc((void **)&flow, bytes))) return e->err;
+    int rc = -1;
+    unsigned timed_out = 0;
+    if (ok(e, cudaMemsetAsync(flow, 0, bytes, e->stream)) &&
+        launch_squarings(s, flow, 0, 1, grid, (long long)wait_cycles) == 0 && check_launch(e) &&
+        ok(e, cudaMemcpyAsync(&timed_out, flow + kFlowTimeout, sizeof timed_out, cudaMemcpyDeviceToHost, e->stream)) &&
+        ok(e, cudaStreamSynchronize(e->stream)))
+        rc = timed_out ? 1 : 0;
+    else if (e->err)
+        rc = e->err;
+    cudaStreamSynchronize(e->stream);
+    cudaFree(flow);
+    return rc;
+}
+
 }  // extern "C"

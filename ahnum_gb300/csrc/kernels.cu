@@ -381,8 +381,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_forward(const Test
 }
 
 // Waits until *ctr >= need, reading it with acquire semantics at GPU scope.  Gives up (returns
-// false) when another CTA has raised *flag, or after about two seconds, raising *flag itself.
-__device__ __noinline__ bool wait_count(const unsigned *ctr, unsigned need, unsigned *flag) {
+// false) when another CTA has raised *flag, or after `limit` SM cycles, raising *flag itself.
+__device__ __noinline__ bool wait_count(const unsigned *ctr, unsigned need, unsigned *flag, long long limit) {
     unsigned v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
     if (v >= need) return true;
@@ -392,7 +392,7 @@ __device__ __noinline__ bool wait_count(const unsigned *ctr, unsigned need, unsi
         asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
         if (v >= need) return true;
         if (*(volatile const unsigned *)flag) return false;
-        if (clock64() - t0 > kWaitCycles) {
+        if (clock64() - t0 > limit) {
             atomicOr(flag, 1u);
             return false;
         }
@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_squarings(const TestDe
                                                         const int *nrows_dev,
                                                         const WorkItem *__restrict__ cols, int ncols,
                                                         const int *ncols_dev, int step0, int nsteps,
-                                                        unsigned *flow) {
+                                                        unsigned *flow, long long wait_limit) {
     extern __shared__ double2 sm[];
     __shared__ unsigned s_q;
     __shared__ int s_ok;
@@ -435,7 +435,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_squarings(const TestDe
                 unsigned need = st * (unsigned)(T.npairs + 2 * T.NG);
                 if (r >= nr) need += (unsigned)T.npairs;
                 if (r >= nr + nc) need += (unsigned)T.NG;
-                ok = wait_count(&flow[kFlowDone + it.test], need, &flow[kFlowTimeout]);
+                ok = wait_count(&flow[kFlowDone + it.test], need, &flow[kFlowTimeout], wait_limit);
             }
             s_q = q;
             s_ok = ok;
@@ -602,10 +602,10 @@ int squarings_grid(const LaunchSet &s, int nsm) {
     }
 }
 
-int launch_squarings(const LaunchSet &s, unsigned *flow, int step0, int nsteps, int grid) {
+int launch_squarings(const LaunchSet &s, unsigned *flow, int step0, int nsteps, int grid, long long wait_limit) {
     if (grid < 1) return -1;
     const size_t smem = squarings_smem(s.row_smem_per_lane * 6, s.col_smem);
-#define KG_SQ_ARGS s.tests, s.rows, s.nrows, s.nrows_dev, s.cols, s.ncols, s.ncols_dev, step0, nsteps, flow
+#define KG_SQ_ARGS s.tests, s.rows, s.nrows, s.nrows_dev, s.cols, s.ncols, s.ncols_dev, step0, nsteps, flow, wait_limit
     switch (s.G) {
     case 2: k_squarings<2><<<grid, s.threads, smem, s.stream>>>(KG_SQ_ARGS); break;
     case 4: k_squarings<4><<<grid, s.threads, smem, s.stream>>>(KG_SQ_ARGS); break;

@@ -17,7 +17,7 @@ constexpr int kMaxDevices = 64;  // devices tracked by the per-device tables of 
 constexpr int kFlowNext = 0;
 constexpr int kFlowTimeout = 1;
 constexpr int kFlowDone = 32;
-// cycles a CTA of k_squarings waits for another CTA's item before it gives up (about 2 s)
+// SM cycles a CTA of k_squarings waits for another CTA's item before it gives up (about 2 s)
 constexpr long long kWaitCycles = 4000000000ll;
 
 // Everything one launch of the pass kernels needs: the test table, the work lists and the
@@ -53,8 +53,10 @@ void launch_fp64_probe(cudaStream_t st, int grid, int block, int iters, double *
 void launch_col_digits(const LaunchSet &s, const double2 *x);
 // Squarings step0 .. step0+nsteps-1 of every test of the lists in one persistent launch
 // (k_squarings) of `grid` CTAs.  `flow` holds kFlowDone + (tests) words, zeroed before the
-// launch.  Returns -1 if grid < 1.
-int launch_squarings(const LaunchSet &s, unsigned *flow, int step0, int nsteps, int grid);
+// launch.  A CTA that waits longer than wait_limit SM cycles for another's item raises
+// flow[kFlowTimeout] and the launch winds down.  Returns -1 if grid < 1.
+int launch_squarings(const LaunchSet &s, unsigned *flow, int step0, int nsteps, int grid,
+                     long long wait_limit = kWaitCycles);
 // CTAs of k_squarings that fit at once on nsm SMs for this set (0 if none); call it outside
 // stream capture.
 int squarings_grid(const LaunchSet &s, int nsm);

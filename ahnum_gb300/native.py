@@ -144,6 +144,7 @@ PROTOTYPES = {
     "kc_stream": (vp, [vp]),
     "kc_shape": (None, [vp, u32p, u32p]),
     "kc_group_width": (C.c_int, [vp]),
+    "kc_engine_wait_selftest": (C.c_int, [vp, C.c_uint64]),
     "kc_square_noalloc": (C.c_int, [vp, vp, vp]),
     "kc_batch_new": (vp, [C.c_int, C.c_uint32, C.c_uint32, C.c_size_t]),
     "kc_batch_free": (None, [vp]),

@@ -74,6 +74,14 @@ void kc_shape(const kc_engine *e, uint32_t *R, uint32_t *C);
 /* Columns per column-pass work unit (2, 4 or 8): an engine created by kc_engine_new spreads each
  * pass of one squaring over the SMs; batch slots use 8. */
 int kc_group_width(const kc_engine *e);
+/* Self-test of the bounded waits of the persistent squaring kernel that batches run (no
+ * counterpart in the reference, whose host threads never wait on one another on a device).
+ * Launches that kernel over engine e's column items without its row items, so every item waits
+ * for work that is not in the queue; each wait gives up after wait_cycles SM cycles, raises the
+ * launch's timeout word and the launch ends.  Nothing is written to e's numbers.  Returns 1 if
+ * the timeout was raised (the expected outcome), 0 if not, or a negative CUDA error.  The
+ * context stays usable afterwards. */
+int kc_engine_wait_selftest(kc_engine *e, uint64_t wait_cycles);
 
 /* ---- a squaring that allocates nothing ---------------------------------------------------
  * No counterpart in the reference (its backends run on the host and never allocate device
