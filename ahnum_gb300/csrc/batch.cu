@@ -89,7 +89,8 @@ struct kc_batch {
     uint32_t graph_B = 0;
     int grid = 0;
     int threads = 128;  // block size of the pass kernels
-    bool persistent = true;       // squaring blocks as persistent k_squarings launches
+    int persistent_mode = -1;     // squaring blocks as k_squarings: -1 chosen per block, 0 never, 1 always
+    bool persistent = false;      // the form of the captured block graph
     uint32_t steps_per_launch = 100;
     unsigned *h_flow = nullptr;   // pinned: the timeout word read back after each block
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -426,10 +427,28 @@ bool fill_lists(kc_batch *b, kc_batch::Lists &l, const std::vector<Entry> &ents)
            bok(b, cudaMemcpyAsync(l.d_cnt, l.h_cnt, 2 * sizeof(int), cudaMemcpyHostToDevice, b->stream));
 }
 
-// (re)capture the B-squaring graph when the lists or shared-memory needs changed
-bool ensure_graph(kc_batch *b, const kc_batch::Lists &l, size_t row_lane, size_t col_smem, bool lists_moved) {
+// Which form the next block's squarings take.  The persistent kernel wins when every CTA has
+// work: on GB300, 1.10-1.13x faster than one launch per pass for 64-256 of the benchmark's tests
+// (1944-7536 column items against 1216 CTAs).  It loses with fewer items than about 1.5 per
+// CTA (0.73-0.93x at 8-32 tests).  It also loses when its shared memory, sized for the longest
+// row of the batch, lets fewer CTAs share an SM than the pass kernels (0.67-0.94x for served
+// mixes that reach C = 576-1024).  The thresholds have some hysteresis, so that a served batch
+// near the boundary does not recapture its graph every block.
+bool choose_persistent(kc_batch *b, const kc_batch::Lists &l, size_t row_lane, size_t col_smem) {
+    if (b->persistent_mode >= 0) return b->persistent_mode == 1;
+    row_lane = std::max(row_lane, b->graph_row_smem);
+    col_smem = std::max(col_smem, b->graph_col_smem);
+    if (kernels_prepare(row_lane * 6, col_smem)) return false;
+    if (squarings_grid(launch_set(b, l, row_lane, col_smem), b->nsm) < b->grid) return false;
+    const double items = std::min(l.h_cnt[0], l.h_cnt[1]);
+    return items >= (b->persistent ? 1.25 : 1.5) * b->grid;
+}
+
+// (re)capture the B-squaring graph when the lists, the shared-memory needs or the form changed
+bool ensure_graph(kc_batch *b, const kc_batch::Lists &l, size_t row_lane, size_t col_smem, bool lists_moved,
+                  bool persistent) {
     if (b->graph && !lists_moved && b->graph_B == b->B && row_lane <= b->graph_row_smem &&
-        col_smem <= b->graph_col_smem)
+        col_smem <= b->graph_col_smem && persistent == b->persistent)
         return true;
     if (b->graph) {
         cudaGraphExecDestroy(b->graph);
@@ -443,10 +462,11 @@ bool ensure_graph(kc_batch *b, const kc_batch::Lists &l, size_t row_lane, size_t
     }
     LaunchSet s = launch_set(b, l, row_lane, col_smem);
     cudaGraph_t g;
-    const int sq_grid = b->persistent ? squarings_grid(s, b->nsm) : 0;
+    b->persistent = persistent;
+    const int sq_grid = persistent ? squarings_grid(s, b->nsm) : 0;
     if (!bok(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal))) return false;
     bool launched = true;
-    if (b->persistent) {
+    if (persistent) {
         // persistent launches of steps_per_launch squarings each; the queue position and the
         // per-test counters start at zero in every launch, the timeout word is left alone
         const size_t done_bytes = (size_t)l.cap_tests * sizeof(unsigned);
@@ -503,9 +523,10 @@ kc_batch *kc_batch_new(int device, uint32_t gerbicz_block, uint32_t gerbicz_bloc
     b->threads = 128;
     if (const char *t = getenv("KITE_GB300_BATCH_THREADS")) b->threads = atoi(t) == 256 ? 256 : 128;
     b->grid = b->nsm * (kThreads * kMinBlocks / b->threads);
-    // A Gerbicz block's squarings run as persistent launches of k_squarings (steps_per_launch
-    // squarings each) unless KITE_GB300_BATCH_PERSISTENT=0 selects three launches per squaring.
-    if (const char *t = getenv("KITE_GB300_BATCH_PERSISTENT")) b->persistent = atoi(t) != 0;
+    // A Gerbicz block's squarings run either as persistent launches of k_squarings
+    // (steps_per_launch squarings each) or as three launches per squaring, chosen per block
+    // (choose_persistent); KITE_GB300_BATCH_PERSISTENT=1 or 0 forces one form.
+    if (const char *t = getenv("KITE_GB300_BATCH_PERSISTENT")) b->persistent_mode = atoi(t) != 0 ? 1 : 0;
     if (const char *t = getenv("KITE_GB300_STEPS_PER_LAUNCH")) {
         const int v = atoi(t);
         if (v > 0) b->steps_per_launch = (uint32_t)v;
@@ -621,7 +642,9 @@ int kc_batch_step(kc_batch *b, uint32_t blocks, double *gpu_ms) {
         if (!fill_lists(b, b->lists[0], sq)) return fail(b, "filling the squaring work lists");
         const bool moved = before != b->lists[0].d_desc ||
                            cap_before != b->lists[0].cap_tests + b->lists[0].cap_rows + b->lists[0].cap_cols;
-        if (!ensure_graph(b, b->lists[0], row_lane, col_smem, moved)) return fail(b, *b->what ? b->what : "capturing the block graph");
+        const bool persistent = choose_persistent(b, b->lists[0], row_lane, col_smem);
+        if (!ensure_graph(b, b->lists[0], row_lane, col_smem, moved, persistent))
+            return fail(b, *b->what ? b->what : "capturing the block graph");
         bok(b, cudaEventRecord(b->ev0, b->stream));
         bok(b, cudaGraphLaunch(b->graph, b->stream));
         // ---- end of block products: d <- d*x (after t <- d) for running Fermat slots,

@@ -183,12 +183,14 @@ def run_reference(args):
 
 # squarings of every test per persistent launch (the batch's default, KITE_GB300_STEPS_PER_LAUNCH)
 STEPS_PER_LAUNCH = 100
-# DRAM bytes (read + write) of one k_squarings launch (100 squarings of this workload's 256
-# tests), from an ncu capture of the same launch: ncu --metrics
-# gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum --clock-control none
-# -k regex:k_squarings -s 2 -c 1 python bench.py --quick --steps 1 --warmup 1 --no-ntt
-# (35.01 GB read + 20.61 GB written)
-K_SQ_DRAM_BYTES = 55.62e9
+# From one ncu capture of a k_squarings launch (100 squarings of this workload's 256 tests):
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,sm__sass_thread_inst_executed_op_
+#   {dfma,dadd,dmul}_pred_on.sum,... --clock-control none -k regex:k_squarings -s 12 -c 1
+#   python bench.py --quick --steps 1 --warmup 1 --no-ntt
+# DRAM: 34.93 GB read + 20.57 GB written.  FP64 lane operations executed (DFMA + DADD + DMUL,
+# active lanes): 47.90e9 (33.90e9 + 9.40e9 + 4.60e9).
+K_SQ_DRAM_BYTES = 55.50e9
+K_SQ_FP64_LANE_OPS = 47.90e9
 K_SQ_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_squarings launch, "
                        "profiles/k_squarings_fermat_batch256.md")
 
@@ -350,6 +352,12 @@ def run_ours(args):
             "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12,
                          "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
                          "traffic": K_SQ_DRAM_BYTES, "traffic_source": K_SQ_TRAFFIC_SOURCE,
+                         # FP64 instructions actually issued (ncu count) against the probe's
+                         # instruction rate (peak / 2: the probe's DFMAs count 2 FLOPs each)
+                         "fp64_issue": {"lane_ops_per_launch": K_SQ_FP64_LANE_OPS,
+                                        "per_second": K_SQ_FP64_LANE_OPS / (msp.value * 1e-3) if msp.value else None,
+                                        "vs_probe_rate": (K_SQ_FP64_LANE_OPS / (msp.value * 1e-3)) / (peak / 2)
+                                        if msp.value and peak else None},
                          "kernel": sq_name,
                          "peak_source": "measured: DFMA dependent-chain kernel on this GPU "
                                         "(MEASURED_PEAKS.json has no FP64 figure)"},
