@@ -529,7 +529,7 @@ kc_batch *kc_batch_new(int device, uint32_t gerbicz_block, uint32_t gerbicz_bloc
     if (const char *t = getenv("KITE_GB300_BATCH_PERSISTENT")) b->persistent_mode = atoi(t) != 0 ? 1 : 0;
     if (const char *t = getenv("KITE_GB300_STEPS_PER_LAUNCH")) {
         const int v = atoi(t);
-        if (v > 0) b->steps_per_launch = (uint32_t)v;
+        if (v > 0) b->steps_per_launch = (uint32_t)std::min(v, 1000);  // queue index stays far below 2^32
     }
     if (!bok(b, cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) || !bok(b, cudaEventCreate(&b->ev0)) ||
         !bok(b, cudaEventCreate(&b->ev1))) {

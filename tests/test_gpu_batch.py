@@ -22,8 +22,15 @@ LLR = [
 ]
 
 
-def test_batch_mixed_fermat_and_llr(lib):
+@pytest.mark.parametrize("form", ["auto", "persistent", "per_pass"])
+def test_batch_mixed_fermat_and_llr(lib, monkeypatch, form):
+    """Both forms of a block (the persistent kernel over one queue, and one launch per pass)
+    give the golden verdicts; `auto` lets the batch choose (per pass, for a batch this small)."""
     from ahnum_gb300.kite import Batch, prp
+    if form == "auto":
+        monkeypatch.delenv("KITE_GB300_BATCH_PERSISTENT", raising=False)
+    else:
+        monkeypatch.setenv("KITE_GB300_BATCH_PERSISTENT", "1" if form == "persistent" else "0")
     with Batch(gerbicz_block=200, gerbicz_blocks=20) as b:
         slots = {}
         for k, n, res in FERMAT:
