@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <mutex>
 
 #include "fft_device.cuh"
@@ -49,6 +50,14 @@ __device__ __forceinline__ void split_pair(double2 &a, double2 &b, double2 w, bo
     a = make_double2(Xr - Yi, Xi + Yr);
     b = make_double2(Xr + Yi, Yr - Xi);
 }
+
+// Programmatic dependent launch: wait until the previous kernel of the stream has completed and
+// its writes are visible, then let the next kernel's CTAs be scheduled while this one runs (they
+// wait here in turn).  A kernel launched without the attribute passes through both at once.
+// The next grid launches only after every CTA of this one has passed here, so its waiting CTAs
+// never hold resources that CTAs of this grid still need.
+__device__ __forceinline__ void pdl_enter() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_leave() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 // One row pair of one test: forward row transforms, split square or product, inverse row
 // transforms, written back in place.  Ends with a barrier after its last global write.
@@ -115,6 +124,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_rows(const TestDesc *_
                                                    const int *nwork_dev, int step, double2 *xo,
                                                    const double2 *yo) {
     extern __shared__ double2 sm[];
+    pdl_enter();
     if (nwork_dev) nwork = *nwork_dev;
     for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
         const WorkItem it = work[wi];
@@ -122,6 +132,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_rows(const TestDesc *_
         if (step >= T.count) continue;
         rows_item<MUL>(T, it.unit, xo ? xo : T.x, MUL ? (yo ? yo : T.y) : nullptr, sm);
     }
+    pdl_leave();
 }
 
 // floor((hi) / k) for a signed 128-bit hi and 0 < k < 2^31, in 32-bit chunks
@@ -307,6 +318,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_inverse(const Test
                                                           int nwork, const int *nwork_dev,
                                                           int step, const double2 *xo) {
     extern __shared__ double2 sm[];
+    pdl_enter();
     if (nwork_dev) nwork = *nwork_dev;
     for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
         const WorkItem it = work[wi];
@@ -314,6 +326,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_inverse(const Test
         if (step >= T.count) continue;
         col_inverse_item<ERR, G>(T, it.unit, step, xo ? xo : T.x, sm);
     }
+    pdl_leave();
 }
 
 // One column group of one test, second half of the column pass: absorb the carry-in,
@@ -371,6 +384,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_forward(const Test
                                                           int nwork, const int *nwork_dev, int step,
                                                           double2 *xo, int use_slots) {
     extern __shared__ double2 sm[];
+    pdl_enter();
     if (nwork_dev) nwork = *nwork_dev;
     for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
         const WorkItem it = work[wi];
@@ -378,6 +392,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_forward(const Test
         if (step >= T.count) continue;
         col_forward_item<G>(T, it.unit, xo ? xo : T.x, use_slots != 0, sm);
     }
+    pdl_leave();
 }
 
 // Waits until *ctr >= need, reading it with acquire semantics at GPU scope.  Gives up (returns
@@ -468,6 +483,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_digits(const TestD
                                                          const WorkItem *__restrict__ work,
                                                          int nwork, const double2 *xo) {
     extern __shared__ double2 sm[];
+    pdl_enter();
     for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
         const WorkItem it = work[wi];
         const TestDesc &T = tests[it.test];
@@ -484,6 +500,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_digits(const TestD
         }
         __syncthreads();
     }
+    pdl_leave();
 }
 
 // x op= y element-wise over n complex values: 0 copy, 1 add, 2 sub
@@ -548,20 +565,50 @@ int kernels_prepare(size_t row_smem, size_t col_smem) {
     return rc;
 }
 
+// Pass kernels launch with programmatic stream serialization (each enters through pdl_enter),
+// so in a stream or graph the next pass's CTAs are scheduled while the previous pass drains.
+// KITE_GB300_PDL=0 launches them plainly.
+static bool pdl_enabled() {
+    static const bool on = [] {
+        const char *t = getenv("KITE_GB300_PDL");
+        return !t || atoi(t) != 0;
+    }();
+    return on;
+}
+
+template <typename... Params, typename... Args>
+static void launch_pass(void (*k)(Params...), int grid, int block, size_t smem, cudaStream_t st, Args... args) {
+    if (!pdl_enabled()) {
+        k<<<grid, block, smem, st>>>(args...);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, static_cast<Params>(args)...);
+}
+
 void launch_rows(const LaunchSet &s, bool mul, double2 *x, const double2 *y, int step) {
     const size_t smem = s.row_smem_per_lane * (mul ? 6 : 4);
     if (mul)
-        k_rows<true><<<s.grid_rows, s.threads, smem, s.stream>>>(s.tests, s.rows, s.nrows, s.nrows_dev, step, x, y);
+        launch_pass(k_rows<true>, s.grid_rows, s.threads, smem, s.stream, s.tests, s.rows, s.nrows, s.nrows_dev, step, x, y);
     else
-        k_rows<false><<<s.grid_rows, s.threads, smem, s.stream>>>(s.tests, s.rows, s.nrows, s.nrows_dev, step, x, y);
+        launch_pass(k_rows<false>, s.grid_rows, s.threads, smem, s.stream, s.tests, s.rows, s.nrows, s.nrows_dev, step, x, y);
 }
 
 template <int G>
 static void col_inverse_g(const LaunchSet &s, bool err, const double2 *x, int step) {
     if (err)
-        k_col_inverse<true, G><<<s.grid_cols, s.threads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x);
+        launch_pass(k_col_inverse<true, G>, s.grid_cols, s.threads, s.col_smem, s.stream, s.tests, s.cols, s.ncols, s.ncols_dev, step, x);
     else
-        k_col_inverse<false, G><<<s.grid_cols, s.threads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x);
+        launch_pass(k_col_inverse<false, G>, s.grid_cols, s.threads, s.col_smem, s.stream, s.tests, s.cols, s.ncols, s.ncols_dev, step, x);
 }
 
 void launch_col_inverse(const LaunchSet &s, bool err, const double2 *x, int step) {
@@ -575,9 +622,9 @@ void launch_col_inverse(const LaunchSet &s, bool err, const double2 *x, int step
 void launch_col_forward(const LaunchSet &s, double2 *x, bool use_slots, int step) {
     const int u = use_slots ? 1 : 0;
     switch (s.G) {
-    case 2: k_col_forward<2><<<s.grid_cols, s.threads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x, u); break;
-    case 4: k_col_forward<4><<<s.grid_cols, s.threads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x, u); break;
-    default: k_col_forward<8><<<s.grid_cols, s.threads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, s.ncols_dev, step, x, u); break;
+    case 2: launch_pass(k_col_forward<2>, s.grid_cols, s.threads, s.col_smem, s.stream, s.tests, s.cols, s.ncols, s.ncols_dev, step, x, u); break;
+    case 4: launch_pass(k_col_forward<4>, s.grid_cols, s.threads, s.col_smem, s.stream, s.tests, s.cols, s.ncols, s.ncols_dev, step, x, u); break;
+    default: launch_pass(k_col_forward<8>, s.grid_cols, s.threads, s.col_smem, s.stream, s.tests, s.cols, s.ncols, s.ncols_dev, step, x, u); break;
     }
 }
 
@@ -617,9 +664,9 @@ int launch_squarings(const LaunchSet &s, unsigned *flow, int step0, int nsteps, 
 
 void launch_col_digits(const LaunchSet &s, const double2 *x) {
     switch (s.G) {
-    case 2: k_col_digits<2><<<s.grid_cols, s.threads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, x); break;
-    case 4: k_col_digits<4><<<s.grid_cols, s.threads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, x); break;
-    default: k_col_digits<8><<<s.grid_cols, s.threads, s.col_smem, s.stream>>>(s.tests, s.cols, s.ncols, x); break;
+    case 2: launch_pass(k_col_digits<2>, s.grid_cols, s.threads, s.col_smem, s.stream, s.tests, s.cols, s.ncols, x); break;
+    case 4: launch_pass(k_col_digits<4>, s.grid_cols, s.threads, s.col_smem, s.stream, s.tests, s.cols, s.ncols, x); break;
+    default: launch_pass(k_col_digits<8>, s.grid_cols, s.threads, s.col_smem, s.stream, s.tests, s.cols, s.ncols, x); break;
     }
 }
 
