@@ -1380,21 +1380,80 @@ int kn_group_add(kn_group *g, kn_engine *e, uint64_t *x) {
     return (int)g->eng.size() - 1;
 }
 
+namespace {
+
+// the group's tables and its graph of kGroupChunk squarings, built if needed
+bool group_prepare(kn_group *g) {
+    if (!group_build(g)) return false;
+    if (!g->graph) {
+        cudaGraph_t graph = nullptr;
+        if (!gok(g, cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal))) return false;
+        for (uint32_t i = 0; i < kGroupChunk; i++) group_square_once(g);
+        if (!gok(g, cudaStreamEndCapture(g->stream, &graph))) return false;
+        const bool ok = gok(g, cudaGraphInstantiate(&g->graph, graph, 0));
+        cudaGraphDestroy(graph);
+        if (!ok) return false;
+        g->graph_len = kGroupChunk;
+    }
+    return true;
+}
+
+// sticky device-side status of every member (a carry that did not settle)
+void group_check_status(kn_group *g) {
+    for (kn_engine *e : g->eng) {
+        int st = 0;
+        cudaMemcpy(&st, e->d_status, sizeof st, cudaMemcpyDeviceToHost);
+        if (st) g->err = -100 - st;
+    }
+}
+
+}  // namespace
+
+int kn_groups_square(kn_group *const *gs, int ng, uint64_t count, float *gpu_ms) {
+    if (!gs || ng < 1) return -1;
+    for (int i = 0; i < ng; i++)
+        if (!gs[i] || gs[i]->err || gs[i]->device != gs[0]->device) return -1;
+    if (ng == 1) return kn_group_square(gs[0], count, gpu_ms);
+    if (!count) return 0;
+    kn_group *g0 = gs[0];
+    cudaSetDevice(g0->device);
+    std::vector<kn_group *> live;
+    for (int i = 0; i < ng; i++) {
+        if (gs[i]->eng.empty()) continue;
+        if (!group_prepare(gs[i])) return -1;
+        live.push_back(gs[i]);
+    }
+    if (live.empty()) return 0;
+    // every stream starts after g0's start event, and g0's stream waits for all at the end
+    bool ok = gok(g0, cudaEventRecord(g0->ev0, g0->stream));
+    for (kn_group *g : live)
+        if (g != g0) ok = ok && gok(g, cudaStreamWaitEvent(g->stream, g0->ev0, 0));
+    uint64_t done = 0;
+    for (; ok && done + kGroupChunk <= count; done += kGroupChunk)
+        for (kn_group *g : live) ok = ok && gok(g, cudaGraphLaunch(g->graph, g->stream));
+    for (; ok && done < count; done++)
+        for (kn_group *g : live) group_square_once(g);
+    for (kn_group *g : live)
+        if (ok && g != g0)
+            ok = gok(g, cudaEventRecord(g->ev1, g->stream)) && gok(g0, cudaStreamWaitEvent(g0->stream, g->ev1, 0));
+    ok = ok && gok(g0, cudaEventRecord(g0->ev1, g0->stream)) && gok(g0, cudaGetLastError()) &&
+         gok(g0, cudaStreamSynchronize(g0->stream));
+    for (kn_group *g : live) {
+        cudaStreamSynchronize(g->stream);
+        group_check_status(g);
+    }
+    if (!ok) return -1;
+    if (gpu_ms) cudaEventElapsedTime(gpu_ms, g0->ev0, g0->ev1);
+    for (kn_group *g : live)
+        if (g->err) return -1;
+    return 0;
+}
+
 int kn_group_square(kn_group *g, uint64_t count, float *gpu_ms) {
     if (!g || g->err) return -1;
     if (g->eng.empty() || !count) return 0;
     cudaSetDevice(g->device);
-    if (!group_build(g)) return -1;
-    if (!g->graph) {
-        cudaGraph_t graph = nullptr;
-        if (!gok(g, cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal))) return -1;
-        for (uint32_t i = 0; i < kGroupChunk; i++) group_square_once(g);
-        if (!gok(g, cudaStreamEndCapture(g->stream, &graph))) return -1;
-        const bool ok = gok(g, cudaGraphInstantiate(&g->graph, graph, 0));
-        cudaGraphDestroy(graph);
-        if (!ok) return -1;
-        g->graph_len = kGroupChunk;
-    }
+    if (!group_prepare(g)) return -1;
     gok(g, cudaEventRecord(g->ev0, g->stream));
     uint64_t done = 0;
     for (; done + g->graph_len <= count; done += g->graph_len)
@@ -1403,11 +1462,7 @@ int kn_group_square(kn_group *g, uint64_t count, float *gpu_ms) {
     gok(g, cudaEventRecord(g->ev1, g->stream));
     if (!gok(g, cudaGetLastError()) || !gok(g, cudaStreamSynchronize(g->stream))) return -1;
     if (gpu_ms) cudaEventElapsedTime(gpu_ms, g->ev0, g->ev1);
-    for (kn_engine *e : g->eng) {
-        int st = 0;
-        cudaMemcpy(&st, e->d_status, sizeof st, cudaMemcpyDeviceToHost);
-        if (st) g->err = -100 - st;
-    }
+    group_check_status(g);
     return g->err ? -1 : 0;
 }
 

@@ -200,6 +200,7 @@ PROTOTYPES = {
     "kn_group_free": (None, [vp]),
     "kn_group_add": (C.c_int, [vp, vp, vp]),
     "kn_group_square": (C.c_int, [vp, C.c_uint64, C.POINTER(C.c_float)]),
+    "kn_groups_square": (C.c_int, [C.POINTER(vp), C.c_int, C.c_uint64, C.POINTER(C.c_float)]),
     "kn_group_mul": (C.c_int, [vp, C.POINTER(vp), C.POINTER(C.c_float)]),
     "kn_group_error": (C.c_int, [vp]),
     # PRST-compatible proofs (include/kite_proof.h)

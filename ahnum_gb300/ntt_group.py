@@ -1,6 +1,6 @@
 """Many tests on the exact integer-NTT engine at once (include/kite_ntt.h, kn_group_*).
 
-  python -m ahnum_gb300.ntt_group [--tests 256] [--squarings 64] [--reps 3] [--seed 3]
+  python -m ahnum_gb300.ntt_group [--tests 256] [--squarings 64] [--reps 3] [--seed 3] [--streams 2]
 
 squares every test's number of the batched workload (k odd in [3, 10^4], n in [300000, 700000],
 seeded PCG64, the benchmark's tests) `squarings` times per timed call and prints the GPU time per
@@ -16,17 +16,45 @@ import statistics
 from . import native
 
 
-class NttGroup:
-    """A kn_group with one engine and one number per test, each number starting at 3."""
+def split_members(members, parts: int, size=lambda m: m):
+    """`members` dealt into `parts` lists of about equal work, largest first."""
+    order = sorted(members, key=size, reverse=True)
+    out = [[] for _ in range(max(1, min(parts, len(order))))]
+    load = [0] * len(out)
+    for m in order:
+        i = load.index(min(load))
+        out[i].append(m)
+        load[i] += size(m)
+    return out
 
-    def __init__(self, tests, device: int = 0, start: int = 3):
+
+def square_groups(lib, groups, count: int) -> float:
+    """kn_groups_square of several groups (one stream each); returns the GPU milliseconds."""
+    arr = (C.c_void_p * len(groups))(*groups)
+    ms = C.c_float(0)
+    if lib.kn_groups_square(arr, len(groups), count, C.byref(ms)) != 0:
+        raise RuntimeError("kn_groups_square failed")
+    return ms.value
+
+
+class NttGroup:
+    """One engine and one number per test, each number starting at 3, in `streams` kn_groups of
+    about equal work that square together, one CUDA stream each."""
+
+    def __init__(self, tests, device: int = 0, start: int = 3, streams: int = 2):
         self.lib = native.load()
-        self.h = self.lib.kn_group_new(device)
-        if not self.h:
-            raise RuntimeError("kn_group_new failed")
-        self.engines, self.nums = [], []
+        self.engines, self.nums, self.groups = [], [], []
         try:
-            for k, n in tests:
+            parts = split_members(list(enumerate(tests)), streams, size=lambda m: m[1][1])
+            member_group = {}
+            for gi, part in enumerate(parts):
+                g = self.lib.kn_group_new(device)
+                if not g:
+                    raise RuntimeError("kn_group_new failed")
+                self.groups.append(g)
+                for i, _ in part:
+                    member_group[i] = g
+            for i, (k, n) in enumerate(tests):
                 e = self.lib.kn_engine_new(k, n, device)
                 if not e:
                     raise RuntimeError(f"kn_engine_new({k}, {n}) failed")
@@ -37,7 +65,7 @@ class NttGroup:
                 self.nums.append(x)
                 limbs = (C.c_uint64 * self.lib.kn_limbs(e))()
                 limbs[0] = start
-                if self.lib.kn_set_limbs(e, x, limbs) != 0 or self.lib.kn_group_add(self.h, e, x) < 0:
+                if self.lib.kn_set_limbs(e, x, limbs) != 0 or self.lib.kn_group_add(member_group[i], e, x) < 0:
                     raise RuntimeError("adding a test to the group failed")
         except Exception:
             self.close()
@@ -52,15 +80,12 @@ class NttGroup:
 
     def square(self, count: int) -> float:
         """Square every member `count` times; returns the GPU milliseconds of the call."""
-        ms = C.c_float(0)
-        if self.lib.kn_group_square(self.h, count, C.byref(ms)) != 0:
-            raise RuntimeError(f"kn_group_square failed ({self.lib.kn_group_error(self.h)})")
-        return ms.value
+        return square_groups(self.lib, self.groups, count)
 
     def close(self):
-        if self.h:
-            self.lib.kn_group_free(self.h)
-            self.h = None
+        for g in self.groups:
+            self.lib.kn_group_free(g)
+        self.groups = []
         for e, x in zip(self.engines, self.nums):
             self.lib.kn_num_free(e, x)
         for e in self.engines:
@@ -76,7 +101,8 @@ class NttGroup:
 
 class NttFermatBatch:
     """Fermat base-a PRP tests of many N = k*2^n-1 on the integer-NTT engine, in lockstep Gerbicz
-    blocks: every block squares all tests' x B times (one group launch set per squaring) and
+    blocks: every block squares all tests' x B times (`streams` groups of about equal work, one
+    CUDA stream each, one launch set per group per squaring) and
     multiplies d <- d*x (one group product); every M blocks, t = d before the block's product is
     checked as x0 * t^(2^B) == d, the reference's check (src/prp.c:407-567), and the verified
     (x, d) kept on the host; a failed check returns every test to its verified state.  A test
@@ -84,9 +110,10 @@ class NttFermatBatch:
     doubled tail (the tail squared twice and compared), as kite_prp does."""
 
     def __init__(self, tests, base: int = 3, block: int = 1000, blocks_per_check: int = 250,
-                 device: int = 0):
+                 device: int = 0, streams: int = 2):
         self.lib = native.load()
         self.base, self.B, self.M, self.device = base, block, blocks_per_check, device
+        self.streams = streams   # the block squarings run as this many groups, one stream each
         self.t = []
         for k, n in tests:
             e = self.lib.kn_engine_new(k, n, device)
@@ -136,6 +163,9 @@ class NttFermatBatch:
         ms = C.c_float(0)
         self._timed(self.lib.kn_group_square(g, count, C.byref(ms)), ms)
 
+    def _square_groups(self, groups, count):
+        self.gpu_ms += square_groups(self.lib, groups, count)
+
     def _mul(self, g, members, which):
         ys = (C.c_void_p * len(members))(*[st[which] for st in members])
         ms = C.c_float(0)
@@ -167,7 +197,9 @@ class NttFermatBatch:
                     self._finish(st)
             if not active or (max_blocks is not None and blocks >= max_blocks):
                 break
-            gx, gd, gt = (self._group(active, w) for w in ("x", "d", "t"))
+            gxs = [self._group(part, "x")
+                   for part in split_members(active, self.streams, size=lambda st: st["n"])]
+            gd, gt = (self._group(active, w) for w in ("d", "t"))
             try:
                 # blocks until the next check, or until a test would leave the lockstep
                 room = min((st["n"] - st["done"]) // self.B for st in active)
@@ -179,7 +211,7 @@ class NttFermatBatch:
                         for st in active:
                             self.lib.kn_copy(st["e"], st["t"], st["d"])
                     before = self.gpu_ms
-                    self._square(gx, self.B)
+                    self._square_groups(gxs, self.B)
                     for st in active:
                         st["done"] += self.B
                         if self.fault and self.fault[0] == st["k"] and st["done"] == self.fault[1]:
@@ -201,7 +233,7 @@ class NttFermatBatch:
                         self._set(st, "d", st["vd"])
                         st["done"] = st.get("vdone", 0)
             finally:
-                for g in (gx, gd, gt):
+                for g in gxs + [gd, gt]:
                     self.lib.kn_group_free(g)
         return [{"k": st["k"], "n": st["n"], "res64": st["res64"], "is_prp": st["is_prp"],
                  "gerbicz_errors": st["gerbicz_errors"]} for st in self.t]
@@ -225,9 +257,9 @@ class NttFermatBatch:
         self.close()
 
 
-def time_steps(tests, squarings: int = 64, reps: int = 3, device: int = 0):
+def time_steps(tests, squarings: int = 64, reps: int = 3, device: int = 0, streams: int = 2):
     """(median seconds per squaring step of all tests, transform lengths)"""
-    with NttGroup(tests, device) as g:
+    with NttGroup(tests, device, streams=streams) as g:
         g.square(16)  # graph capture, clocks
         times = [g.square(squarings) * 1e-3 / squarings for _ in range(reps)]
         return statistics.median(times), g.transform_lengths()
@@ -243,10 +275,11 @@ def main():
     ap.add_argument("--squarings", type=int, default=64)
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--seed", type=int, default=bench.SEED)
+    ap.add_argument("--streams", type=int, default=2, help="groups squared together, one stream each")
     args = ap.parse_args()
     tests = bench.workload(seed=args.seed, count=args.tests)
-    t, lengths = time_steps(tests, args.squarings, args.reps)
-    print(json.dumps({"tests": len(tests), "ms_per_squaring_step": t * 1e3,
+    t, lengths = time_steps(tests, args.squarings, args.reps, streams=args.streams)
+    print(json.dumps({"tests": len(tests), "streams": args.streams, "ms_per_squaring_step": t * 1e3,
                       "us_per_test_squaring": t * 1e6 / len(tests),
                       "transform_lengths": {str(k): v for k, v in lengths.items()}}))
 

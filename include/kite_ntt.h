@@ -76,6 +76,11 @@ kn_group *kn_group_new(int device);
 void kn_group_free(kn_group *g);
 int kn_group_add(kn_group *g, kn_engine *e, uint64_t *x);
 int kn_group_square(kn_group *g, uint64_t count, float *gpu_ms);
+/* kn_group_square of ng groups of the same device at once (no counterpart in the reference's
+ * prototype, which squares one group per command buffer): each group's graphs go to its own
+ * stream, so one group's latency-bound reduction overlaps another's transforms.  gpu_ms
+ * receives the time from the common start to the last group's end. */
+int kn_groups_square(kn_group *const *gs, int ng, uint64_t count, float *gpu_ms);
 /* Every member's number times ys[i] (members in the order they were added; ys[i] a number of
  * member i's engine, distinct from its own number). */
 int kn_group_mul(kn_group *g, const uint64_t *const *ys, float *gpu_ms);
