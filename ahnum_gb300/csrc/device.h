@@ -36,8 +36,9 @@ struct FftPlan {
     int off[kMaxStages] = {};
 };
 
-// Everything a kernel needs for one test (one modulus).  Lives in device memory.
-struct TestDesc {
+// Everything a kernel needs for one test (one modulus).  Lives in device memory; a kernel copies
+// the descriptor of the item it works on into shared memory (16-byte chunks, hence alignas).
+struct alignas(16) TestDesc {
     // shape
     int L, H, R, C, NG;      // NG = C / G column groups
     int G;                   // columns per column group: 2, 4 or 8 (2G digits per row segment)

@@ -59,6 +59,18 @@ __device__ __forceinline__ void split_pair(double2 &a, double2 &b, double2 w, bo
 __device__ __forceinline__ void pdl_enter() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_leave() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
+// The work item's test descriptor, copied into shared memory.  An item reads the descriptor's
+// fields (plans, table pointers, sizes) again at every stage, and from shared memory those
+// reads stay off the texture path that the tables' own loads queue on.  Every thread of the
+// block calls this after the previous item's last barrier; it ends with a barrier.
+__device__ __forceinline__ const TestDesc &stage_desc(const TestDesc *tests, int t, TestDesc *s) {
+    const int4 *src = reinterpret_cast<const int4 *>(tests + t);
+    int4 *dst = reinterpret_cast<int4 *>(s);
+    for (int i = threadIdx.x; i < (int)(sizeof(TestDesc) / 16); i += blockDim.x) dst[i] = __ldg(src + i);
+    __syncthreads();
+    return *s;
+}
+
 // One row pair of one test: forward row transforms, split square or product, inverse row
 // transforms, written back in place.  Ends with a barrier after its last global write.
 template <bool MUL>
@@ -124,12 +136,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_rows(const TestDesc *_
                                                    const int *nwork_dev, int step, double2 *xo,
                                                    const double2 *yo) {
     extern __shared__ double2 sm[];
+    __shared__ TestDesc s_desc;
     pdl_enter();
     if (nwork_dev) nwork = *nwork_dev;
     for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
         const WorkItem it = work[wi];
-        const TestDesc &T = tests[it.test];
-        if (step >= T.count) continue;
+        if (step >= tests[it.test].count) continue;
+        const TestDesc &T = stage_desc(tests, it.test, &s_desc);
         rows_item<MUL>(T, it.unit, xo ? xo : T.x, MUL ? (yo ? yo : T.y) : nullptr, sm);
     }
     pdl_leave();
@@ -318,12 +331,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_inverse(const Test
                                                           int nwork, const int *nwork_dev,
                                                           int step, const double2 *xo) {
     extern __shared__ double2 sm[];
+    __shared__ TestDesc s_desc;
     pdl_enter();
     if (nwork_dev) nwork = *nwork_dev;
     for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
         const WorkItem it = work[wi];
-        const TestDesc &T = tests[it.test];
-        if (step >= T.count) continue;
+        if (step >= tests[it.test].count) continue;
+        const TestDesc &T = stage_desc(tests, it.test, &s_desc);
         col_inverse_item<ERR, G>(T, it.unit, step, xo ? xo : T.x, sm);
     }
     pdl_leave();
@@ -384,12 +398,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_forward(const Test
                                                           int nwork, const int *nwork_dev, int step,
                                                           double2 *xo, int use_slots) {
     extern __shared__ double2 sm[];
+    __shared__ TestDesc s_desc;
     pdl_enter();
     if (nwork_dev) nwork = *nwork_dev;
     for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
         const WorkItem it = work[wi];
-        const TestDesc &T = tests[it.test];
-        if (step >= T.count) continue;
+        if (step >= tests[it.test].count) continue;
+        const TestDesc &T = stage_desc(tests, it.test, &s_desc);
         col_forward_item<G>(T, it.unit, xo ? xo : T.x, use_slots != 0, sm);
     }
     pdl_leave();
@@ -432,6 +447,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_squarings(const TestDe
                                                         const int *ncols_dev, int step0, int nsteps,
                                                         unsigned *flow, long long wait_limit) {
     extern __shared__ double2 sm[];
+    __shared__ TestDesc s_desc;
     __shared__ unsigned s_q;
     __shared__ int s_ok;
     const unsigned nr = (unsigned)(nrows_dev ? *nrows_dev : nrows);
@@ -460,7 +476,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_squarings(const TestDe
         if (q >= total || !s_ok) return;
         const unsigned st = q / per_step, r = q % per_step;
         const WorkItem it = r < nr ? rows[r] : cols[(r - nr) % nc];
-        const TestDesc &T = tests[it.test];
+        const TestDesc &T = stage_desc(tests, it.test, &s_desc);
         const int step = step0 + (int)st;
         if (step < T.count) {
             if (r < nr)
@@ -483,10 +499,11 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_digits(const TestD
                                                          const WorkItem *__restrict__ work,
                                                          int nwork, const double2 *xo) {
     extern __shared__ double2 sm[];
+    __shared__ TestDesc s_desc;
     pdl_enter();
     for (int wi = blockIdx.x; wi < nwork; wi += gridDim.x) {
         const WorkItem it = work[wi];
-        const TestDesc &T = tests[it.test];
+        const TestDesc &T = stage_desc(tests, it.test, &s_desc);
         const double2 *x = xo ? xo : T.x;
         const int R = T.R, C = T.C, g = it.unit;
         load_columns_conj<G>(T, x, g, sm);
