@@ -187,9 +187,9 @@ STEPS_PER_LAUNCH = 100
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,sm__sass_thread_inst_executed_op_
 #   {dfma,dadd,dmul}_pred_on.sum,... --clock-control none -k regex:k_squarings -s 12 -c 1
 #   python bench.py --quick --steps 1 --warmup 1 --no-ntt
-# DRAM: 34.93 GB read + 20.57 GB written.  FP64 lane operations executed (DFMA + DADD + DMUL,
+# DRAM: 34.99 GB read + 20.57 GB written.  FP64 lane operations executed (DFMA + DADD + DMUL,
 # active lanes): 47.90e9 (33.90e9 + 9.40e9 + 4.60e9).
-K_SQ_DRAM_BYTES = 55.50e9
+K_SQ_DRAM_BYTES = 55.57e9
 K_SQ_FP64_LANE_OPS = 47.90e9
 K_SQ_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_squarings launch, "
                        "profiles/k_squarings_fermat_batch256.md")
