@@ -941,6 +941,44 @@ int kc_batch_profile_steps(kc_batch *b, uint32_t squarings, double *ms, double *
     return rc ? rc : b->err;
 }
 
+double kc_fp64_probe_rate(int device, int blocks_per_sm, int threads, int chains, int op) {
+    if (device < 0 && cudaGetDevice(&device) != cudaSuccess) return -1;
+    if (blocks_per_sm < 1 || blocks_per_sm > 32 || (threads != 128 && threads != 256)) return -1;
+    cudaSetDevice(device);
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    cudaStream_t st;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return -1;
+    cudaEvent_t a, c;
+    cudaEventCreate(&a);
+    cudaEventCreate(&c);
+    double *out = nullptr;
+    double best = -1;
+    const int grid = nsm * blocks_per_sm, iters = 32768 / chains;
+    if (cudaMalloc((void **)&out, sizeof(double)) == cudaSuccess &&
+        launch_fp64_probe_var(st, grid, threads, iters, chains, op, out) == 0) {  // warm-up
+        best = 0;
+        for (int r = 0; r < 3; r++) {
+            cudaEventRecord(a, st);
+            launch_fp64_probe_var(st, grid, threads, iters, chains, op, out);
+            cudaEventRecord(c, st);
+            if (cudaEventSynchronize(c) != cudaSuccess) {
+                best = -1;
+                break;
+            }
+            float ms = 0;
+            cudaEventElapsedTime(&ms, a, c);
+            const double lanes = (double)chains * iters * grid * threads;
+            if (ms > 0) best = std::max(best, lanes / (ms * 1e-3));
+        }
+    }
+    cudaFree(out);
+    cudaEventDestroy(a);
+    cudaEventDestroy(c);
+    cudaStreamDestroy(st);
+    return best;
+}
+
 double kc_fp64_peak(int device) {
     if (device < 0 && cudaGetDevice(&device) != cudaSuccess) return 0;
     cudaSetDevice(device);

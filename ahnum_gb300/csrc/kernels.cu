@@ -706,6 +706,39 @@ __global__ void k_fp64_probe(double *out, int iters) {
     if (s > 1e300) out[0] = s;
 }
 
+// The probe's variants for kc_fp64_probe_rate: CH independent chains per thread of one FP64
+// opcode (0 DFMA, 1 DMUL, 2 DADD).
+template <int CH, int OP>
+__global__ void k_fp64_probe_var(double *out, int iters) {
+    double a[CH];
+#pragma unroll
+    for (int c = 0; c < CH; c++) a[c] = threadIdx.x * 1e-9 + c;
+    const double m = 0.999999999, k = 1e-12;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int c = 0; c < CH; c++) a[c] = OP == 0 ? fma(a[c], m, k) : OP == 1 ? a[c] * m : a[c] + k;
+    }
+    double s = 0;
+#pragma unroll
+    for (int c = 0; c < CH; c++) s += a[c];
+    if (s > 1e300) out[0] = s;
+}
+
+int launch_fp64_probe_var(cudaStream_t st, int grid, int block, int iters, int chains, int op, double *out) {
+#define KG_PROBE(CH, OP) k_fp64_probe_var<CH, OP><<<grid, block, 0, st>>>(out, iters)
+    if (op < 0 || op > 2) return -1;
+    switch (chains * 4 + op) {
+    case 4 * 4 + 0: KG_PROBE(4, 0); break;
+    case 8 * 4 + 0: KG_PROBE(8, 0); break;
+    case 16 * 4 + 0: KG_PROBE(16, 0); break;
+    case 8 * 4 + 1: KG_PROBE(8, 1); break;
+    case 8 * 4 + 2: KG_PROBE(8, 2); break;
+    default: return -1;
+    }
+#undef KG_PROBE
+    return 0;
+}
+
 void launch_fp64_probe(cudaStream_t st, int grid, int block, int iters, double *out) {
     k_fp64_probe<<<grid, block, 0, st>>>(out, iters);
 }

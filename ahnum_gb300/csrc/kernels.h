@@ -50,6 +50,9 @@ void launch_col_forward(const LaunchSet &s, double2 *x, bool use_slots, int step
 // FP64 FMA throughput probe: `iters` dependent-chain DFMAs per thread over grid x block;
 // the result is written to out[0] only if the chains overflow (never).
 void launch_fp64_probe(cudaStream_t st, int grid, int block, int iters, double *out);
+// The probe with `chains` chains per thread (4, 8 or 16 for DFMA; 8 for DMUL and DADD) of
+// opcode op (0 DFMA, 1 DMUL, 2 DADD); -1 for a combination it does not have.
+int launch_fp64_probe_var(cudaStream_t st, int grid, int block, int iters, int chains, int op, double *out);
 void launch_col_digits(const LaunchSet &s, const double2 *x);
 // Squarings step0 .. step0+nsteps-1 of every test of the lists in one persistent launch
 // (k_squarings) of `grid` CTAs.  `flow` holds kFlowDone + (tests) words, zeroed before the

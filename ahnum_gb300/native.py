@@ -159,6 +159,7 @@ PROTOTYPES = {
     "kc_batch_error": (C.c_int, [vp]),
     "kc_batch_error_string": (C.c_char_p, [vp]),
     "kc_fp64_peak": (C.c_double, [C.c_int]),
+    "kc_fp64_probe_rate": (C.c_double, [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
     "kc_batch_profile": (C.c_int, [vp, C.c_uint32, dp, dp]),
     "kc_batch_profile_steps": (C.c_int, [vp, C.c_uint32, dp, dp]),
     "kc_batch_read": (C.c_int, [vp, C.c_int, u64p]),

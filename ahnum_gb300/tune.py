@@ -223,11 +223,25 @@ def main():
     c.add_argument("numbers", nargs="+", help="K:N pairs")
     c.add_argument("--squarings", type=int, default=200)
     c.add_argument("--out")
+    f = sub.add_parser("fp64", help="the FP64 probe in several shapes and opcodes (lane ops per second)")
+    f.add_argument("--device", type=int, default=0)
     b = sub.add_parser("roundoff")
     b.add_argument("lengths", type=int, nargs="+")
     b.add_argument("--k", type=int, default=9999)
     b.add_argument("--squarings", type=int, default=500)
     args = ap.parse_args()
+    if args.cmd == "fp64":
+        lib = native.load()
+        print("| opcode | chains per thread | blocks per SM x threads | G lane ops/s | TFLOP/s (FMA = 2) |")
+        print("|---|---|---|---|---|")
+        for op, chains, bps, thr in ((0, 8, 4, 256), (0, 8, 8, 256), (0, 16, 4, 256), (0, 16, 8, 256),
+                                     (0, 4, 8, 256), (0, 8, 2, 256), (0, 8, 16, 128), (1, 8, 8, 256),
+                                     (2, 8, 8, 256)):
+            r = lib.kc_fp64_probe_rate(args.device, bps, thr, chains, op)
+            name = ("DFMA", "DMUL", "DADD")[op]
+            tf = f"{2 * r / 1e12:.4f}" if op == 0 else "-"
+            print(f"| {name} | {chains} | {bps} x {thr} | {r / 1e9:.1f} | {tf} |", flush=True)
+        return
     if args.cmd == "shapes":
         out = open(args.out, "w") if args.out else None
         try:

@@ -179,6 +179,11 @@ int kc_batch_profile_steps(kc_batch *b, uint32_t squarings, double *ms, double *
 /* Measured FP64 FMA throughput of `device` in FLOP/s (2 per FMA), from a dependent-chain DFMA
  * kernel timed with CUDA events: the roofline denominator of this FP64-bound path. */
 double kc_fp64_peak(int device);
+/* The same probe in other shapes, for checking that kc_fp64_peak is the pipe's rate and not the
+ * probe's: blocks_per_sm x threads (128 or 256) per SM, `chains` independent chains per thread
+ * (4, 8 or 16 for DFMA, 8 for the others) of opcode op (0 DFMA, 1 DMUL, 2 DADD).  Returns FP64
+ * lane operations per second (an FMA counts once), or -1. */
+double kc_fp64_probe_rate(int device, int blocks_per_sm, int threads, int chains, int op);
 
 /* ---- per-length tuning (replaces `kite tune`, tools/kite.c:274-326 and src/ctx.c:35-92) ------
  * The four-step shape H = R*C of each FFT length can be chosen by measurement instead of the
