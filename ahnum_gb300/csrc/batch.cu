@@ -66,6 +66,8 @@ size_t slot_bytes(uint32_t L, uint32_t R, uint32_t NG) {
 
 }  // namespace
 
+constexpr int kMaxParts = 4;  // most streams a split block uses
+
 struct kc_batch {
     int device = 0;
     int nsm = 0;
@@ -74,14 +76,15 @@ struct kc_batch {
     double maxround = 0.40;
     size_t budget = 0, in_use = 0;
     std::vector<Slot> slots;
-    // device and pinned host mirrors: [0] squaring blocks, [1] product passes
+    // device and pinned host mirrors of the work lists
     struct Lists {
         int cap_tests = 0, cap_rows = 0, cap_cols = 0;
         TestDesc *d_desc = nullptr, *h_desc = nullptr;
         WorkItem *d_rows = nullptr, *h_rows = nullptr, *d_cols = nullptr, *h_cols = nullptr;
         int *d_cnt = nullptr, *h_cnt = nullptr;
         unsigned *d_flow = nullptr;  // control words of the persistent kernel (kernels.h)
-    } lists[2];
+    } lists[2 + kMaxParts - 1];  // [0] squaring blocks (part 0 of a split block), [1] products,
+                                 // [2 ..] parts 1 .. of a split block
     unsigned long long *h_err = nullptr;  // pinned, one per slot
     int cap_err = 0;
     cudaGraphExec_t graph = nullptr;
@@ -89,8 +92,13 @@ struct kc_batch {
     uint32_t graph_B = 0;
     int grid = 0;
     int threads = 128;  // block size of the pass kernels
-    int persistent_mode = -1;     // squaring blocks as k_squarings: -1 chosen per block, 0 never, 1 always
-    bool persistent = false;      // the form of the captured block graph
+    bool persistent = false;      // squaring blocks as the persistent kernel k_squarings
+    int parts = 3;                // per-pass blocks of 2+ tests in this many parts, one stream each
+    int form = -1;                // the form of the captured block graph (BlockForm)
+    int graph_parts = 0;          // its number of parts
+    cudaStream_t pstream[kMaxParts] = {};  // [0] is `stream`; [1 ..] the other parts of a split block
+    cudaEvent_t fork = nullptr;            // split blocks: the other streams start after it
+    cudaEvent_t join[kMaxParts] = {};      //   and `stream` waits for each of theirs
     uint32_t steps_per_launch = 100;
     unsigned *h_flow = nullptr;   // pinned: the timeout word read back after each block
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -427,29 +435,31 @@ bool fill_lists(kc_batch *b, kc_batch::Lists &l, const std::vector<Entry> &ents)
            bok(b, cudaMemcpyAsync(l.d_cnt, l.h_cnt, 2 * sizeof(int), cudaMemcpyHostToDevice, b->stream));
 }
 
-// Which form the next block's squarings take.  The persistent kernel wins when every CTA has
-// work: on GB300, 1.10-1.13x faster than one launch per pass for 64-256 of the benchmark's tests
-// (1944-7536 column items against 1216 CTAs).  It loses with fewer items than about 1.5 per
-// CTA (0.73-0.93x at 8-32 tests).  It also loses when its shared memory, sized for the longest
-// row of the batch, lets fewer CTAs share an SM than the pass kernels (0.67-0.94x for served
-// mixes that reach C = 576-1024).  The thresholds have some hysteresis, so that a served batch
-// near the boundary does not recapture its graph every block.
-bool choose_persistent(kc_batch *b, const kc_batch::Lists &l, size_t row_lane, size_t col_smem) {
-    if (b->persistent_mode >= 0) return b->persistent_mode == 1;
-    row_lane = std::max(row_lane, b->graph_row_smem);
-    col_smem = std::max(col_smem, b->graph_col_smem);
-    if (kernels_prepare(row_lane * 6, col_smem)) return false;
-    if (squarings_grid(launch_set(b, l, row_lane, col_smem), b->nsm) < b->grid) return false;
-    const double items = std::min(l.h_cnt[0], l.h_cnt[1]);
-    return items >= (b->persistent ? 1.25 : 1.5) * b->grid;
-}
+// The forms a block's squarings take: one launch per pass over all slots; the persistent kernel
+// over all slots; or one launch per pass over `parts` groups of slots of about equal work, each
+// on its own stream (forked and joined inside the graph), so that the groups fill one another's
+// launch tails and low-occupancy passes.  Measured on GB300, ms per squaring of the batch:
+//
+//   tests (workload)     persistent  per pass  2 parts  3 parts  4 parts
+//   32 (benchmark's)       0.159      0.148     0.137    0.132    0.129
+//   64                     0.262      0.287     0.231    0.230    0.230
+//   256                    0.906      1.010     0.893    0.892    0.895
+//   16 (served mix)        0.233      0.229     0.220    0.213    0.213
+//   48                     0.541      0.495     0.429    0.422    0.421
+//
+// So a block of two or more slots is split in three parts (KITE_GB300_BATCH_SPLIT=P picks P, 1
+// keeps one stream), and the persistent kernel runs only when KITE_GB300_BATCH_PERSISTENT=1
+// asks for it.
+enum BlockForm { kPerPass = 0, kPersistent = 1, kSplit = 2 };
+
+kc_batch::Lists &part_lists(kc_batch *b, int p) { return p == 0 ? b->lists[0] : b->lists[1 + p]; }
 
 // (re)capture the B-squaring graph when the lists, the shared-memory needs or the form changed
-bool ensure_graph(kc_batch *b, const kc_batch::Lists &l, size_t row_lane, size_t col_smem, bool lists_moved,
-                  bool persistent) {
+bool ensure_graph(kc_batch *b, size_t row_lane, size_t col_smem, bool lists_moved, int form, int parts) {
     if (b->graph && !lists_moved && b->graph_B == b->B && row_lane <= b->graph_row_smem &&
-        col_smem <= b->graph_col_smem && persistent == b->persistent)
+        col_smem <= b->graph_col_smem && form == b->form && parts == b->graph_parts)
         return true;
+    const kc_batch::Lists &l = b->lists[0];
     if (b->graph) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
@@ -462,11 +472,12 @@ bool ensure_graph(kc_batch *b, const kc_batch::Lists &l, size_t row_lane, size_t
     }
     LaunchSet s = launch_set(b, l, row_lane, col_smem);
     cudaGraph_t g;
-    b->persistent = persistent;
-    const int sq_grid = persistent ? squarings_grid(s, b->nsm) : 0;
+    b->form = form;
+    b->graph_parts = parts;
+    const int sq_grid = form == kPersistent ? squarings_grid(s, b->nsm) : 0;
     if (!bok(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal))) return false;
     bool launched = true;
-    if (persistent) {
+    if (form == kPersistent) {
         // persistent launches of steps_per_launch squarings each; the queue position and the
         // per-test counters start at zero in every launch, the timeout word is left alone
         const size_t done_bytes = (size_t)l.cap_tests * sizeof(unsigned);
@@ -476,6 +487,25 @@ bool ensure_graph(kc_batch *b, const kc_batch::Lists &l, size_t row_lane, size_t
                        bok(b, cudaMemsetAsync(l.d_flow + kFlowDone, 0, done_bytes, b->stream)) &&
                        launch_squarings(s, l.d_flow, (int)j, (int)n, sq_grid) == 0;
         }
+    } else if (form == kSplit) {
+        // part 0 on the batch stream, part p on pstream[p], forked and joined by events
+        LaunchSet ps[kMaxParts];
+        for (int p = 0; p < parts; p++) {
+            ps[p] = launch_set(b, part_lists(b, p), row_lane, col_smem);
+            ps[p].stream = b->pstream[p];
+        }
+        launched = bok(b, cudaEventRecord(b->fork, b->stream));
+        for (int p = 1; p < parts && launched; p++) launched = bok(b, cudaStreamWaitEvent(b->pstream[p], b->fork, 0));
+        for (uint32_t j = 0; j < b->B && launched; j++) {
+            for (int p = 0; p < parts; p++) {
+                launch_rows(ps[p], false, nullptr, nullptr, (int)j);
+                launch_col_inverse(ps[p], true, nullptr, (int)j);
+                launch_col_forward(ps[p], nullptr, true, (int)j);
+            }
+        }
+        for (int p = 1; p < parts && launched; p++)
+            launched = bok(b, cudaEventRecord(b->join[p], b->pstream[p])) &&
+                       bok(b, cudaStreamWaitEvent(b->stream, b->join[p], 0));
     } else {
         for (uint32_t j = 0; j < b->B; j++) {
             launch_rows(s, false, nullptr, nullptr, (int)j);
@@ -486,7 +516,7 @@ bool ensure_graph(kc_batch *b, const kc_batch::Lists &l, size_t row_lane, size_t
     if (!bok(b, cudaStreamEndCapture(b->stream, &g))) return false;
     if (!launched) {
         cudaGraphDestroy(g);
-        b->what = "launching the persistent squaring kernel";
+        b->what = "capturing the block's launches";
         return false;
     }
     bool ok = bok(b, cudaGraphInstantiate(&b->graph, g, 0));
@@ -523,19 +553,28 @@ kc_batch *kc_batch_new(int device, uint32_t gerbicz_block, uint32_t gerbicz_bloc
     b->threads = 128;
     if (const char *t = getenv("KITE_GB300_BATCH_THREADS")) b->threads = atoi(t) == 256 ? 256 : 128;
     b->grid = b->nsm * (kThreads * kMinBlocks / b->threads);
-    // A Gerbicz block's squarings run either as persistent launches of k_squarings
-    // (steps_per_launch squarings each) or as three launches per squaring, chosen per block
-    // (choose_persistent); KITE_GB300_BATCH_PERSISTENT=1 or 0 forces one form.
-    if (const char *t = getenv("KITE_GB300_BATCH_PERSISTENT")) b->persistent_mode = atoi(t) != 0 ? 1 : 0;
+    // A Gerbicz block's squarings run as pass launches in parts on several streams (BlockForm);
+    // KITE_GB300_BATCH_PERSISTENT=1 runs them as persistent launches of k_squarings instead
+    // (steps_per_launch squarings each).
+    if (const char *t = getenv("KITE_GB300_BATCH_PERSISTENT")) b->persistent = atoi(t) != 0;
+    // KITE_GB300_BATCH_SPLIT=P splits per-pass blocks into P parts (1 or 0: one stream)
+    if (const char *t = getenv("KITE_GB300_BATCH_SPLIT")) b->parts = std::max(1, std::min(atoi(t), kMaxParts));
     if (const char *t = getenv("KITE_GB300_STEPS_PER_LAUNCH")) {
         const int v = atoi(t);
         if (v > 0) b->steps_per_launch = (uint32_t)std::min(v, 1000);  // queue index stays far below 2^32
     }
     if (!bok(b, cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) || !bok(b, cudaEventCreate(&b->ev0)) ||
-        !bok(b, cudaEventCreate(&b->ev1))) {
+        !bok(b, cudaEventCreate(&b->ev1)) || !bok(b, cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming))) {
         kc_batch_free(b);
         return nullptr;
     }
+    b->pstream[0] = b->stream;
+    for (int p = 1; p < kMaxParts; p++)
+        if (!bok(b, cudaStreamCreateWithFlags(&b->pstream[p], cudaStreamNonBlocking)) ||
+            !bok(b, cudaEventCreateWithFlags(&b->join[p], cudaEventDisableTiming))) {
+            kc_batch_free(b);
+            return nullptr;
+        }
     return b;
 }
 
@@ -545,13 +584,19 @@ void kc_batch_free(kc_batch *b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     for (auto &s : b->slots) release_slot(b, s);
     if (b->graph) cudaGraphExecDestroy(b->graph);
-    free_lists(b->lists[0]);
-    free_lists(b->lists[1]);
+    for (int p = 1; p < kMaxParts; p++)
+        if (b->pstream[p]) cudaStreamSynchronize(b->pstream[p]);
+    for (auto &l : b->lists) free_lists(l);
     if (b->h_err) cudaFreeHost(b->h_err);
     if (b->h_flow) cudaFreeHost(b->h_flow);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
+    for (int p = 1; p < kMaxParts; p++) {
+        if (b->pstream[p]) cudaStreamDestroy(b->pstream[p]);
+        if (b->join[p]) cudaEventDestroy(b->join[p]);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
     delete b;
 }
 
@@ -637,13 +682,34 @@ int kc_batch_step(kc_batch *b, uint32_t blocks, double *gpu_ms) {
         if (sq.empty()) break;
         size_t row_lane, col_smem;
         max_smem(b, row_lane, col_smem);
-        const int cap_before = b->lists[0].cap_tests + b->lists[0].cap_rows + b->lists[0].cap_cols;
-        TestDesc *before = b->lists[0].d_desc;
-        if (!fill_lists(b, b->lists[0], sq)) return fail(b, "filling the squaring work lists");
-        const bool moved = before != b->lists[0].d_desc ||
-                           cap_before != b->lists[0].cap_tests + b->lists[0].cap_rows + b->lists[0].cap_cols;
-        const bool persistent = choose_persistent(b, b->lists[0], row_lane, col_smem);
-        if (!ensure_graph(b, b->lists[0], row_lane, col_smem, moved, persistent))
+        int form = b->persistent ? kPersistent : kPerPass;
+        const int nparts = form == kPerPass ? std::min<int>(b->parts, (int)sq.size()) : 1;
+        if (nparts >= 2) form = kSplit;
+        // the lists: all slots in part 0, or a split block's parts of about equal work (row pairs
+        // and column groups), largest slots first, each to the part with the least work so far
+        std::vector<Entry> part[kMaxParts];
+        if (form == kSplit) {
+            std::vector<Entry> order = sq;
+            auto work = [](const Entry &en) { return en.s->e->plan->pairs.size() + (size_t)en.s->e->NG; };
+            std::stable_sort(order.begin(), order.end(), [&](const Entry &a, const Entry &c) { return work(a) > work(c); });
+            size_t load[kMaxParts] = {};
+            for (auto &en : order) {
+                const int h = (int)(std::min_element(load, load + nparts) - load);
+                part[h].push_back(en);
+                load[h] += work(en);
+            }
+        } else {
+            part[0] = sq;
+        }
+        bool moved = false;
+        for (int p = 0; p < nparts || p == 0; p++) {
+            kc_batch::Lists &l = part_lists(b, p);
+            const int cap_before = l.cap_tests + l.cap_rows + l.cap_cols;
+            TestDesc *before = l.d_desc;
+            if (!fill_lists(b, l, part[p])) return fail(b, "filling the squaring work lists");
+            moved = moved || before != l.d_desc || cap_before != l.cap_tests + l.cap_rows + l.cap_cols;
+        }
+        if (!ensure_graph(b, row_lane, col_smem, moved, form, std::max(nparts, 1)))
             return fail(b, *b->what ? b->what : "capturing the block graph");
         bok(b, cudaEventRecord(b->ev0, b->stream));
         bok(b, cudaGraphLaunch(b->graph, b->stream));
@@ -681,14 +747,14 @@ int kc_batch_step(kc_batch *b, uint32_t blocks, double *gpu_ms) {
             b->d2h += 8;
             bok(b, cudaMemsetAsync(s.e->d_maxerr, 0, 8, b->stream));
         }
-        if (b->persistent) {
+        if (b->form == kPersistent) {
             if (!b->h_flow && !bok(b, cudaMallocHost((void **)&b->h_flow, sizeof(unsigned)))) return b->err;
             bok(b, cudaMemcpyAsync(b->h_flow, b->lists[0].d_flow + kFlowTimeout, sizeof(unsigned),
                                    cudaMemcpyDeviceToHost, b->stream));
             b->d2h += sizeof(unsigned);
         }
         if (!bok(b, cudaStreamSynchronize(b->stream))) return b->err;
-        if (b->persistent && *b->h_flow) {
+        if (b->form == kPersistent && *b->h_flow) {
             // a CTA gave up waiting for another's item: the block's numbers are not to be trusted
             b->err = -(int)cudaErrorLaunchTimeout;
             return fail(b, "a CTA of the persistent squaring kernel timed out waiting for another's item");

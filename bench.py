@@ -6,9 +6,9 @@ k uniform odd in [3, 10^4], n uniform integer in [300000, 700000] (numpy PCG64, 
 the FFT length the reference's length chooser picks (16K-56K words).  Synthetic, seeded: the
 reference publishes no benchmark suite.
 
-A step is one Gerbicz block of every test: B = 1000 squarings of each test's x (one CUDA graph
-of ten persistent launches of 100 squarings each over all 256 tests) plus the block's product
-d <- d*x.  The check of every M = 250
+A step is one Gerbicz block of every test: B = 1000 squarings of each test's x (one CUDA graph:
+the tests in three parts of about equal work, each part's 3000 pass launches on its own stream)
+plus the block's product d <- d*x.  The check of every M = 250
 blocks (another B squarings and a product) is charged analytically, as a factor (1 + 1/M).
 Throughput is the steady state of a served batch whose slots are refilled with tests of the same
 distribution:  tests/hour = 3600 * slots * B / (T_block * (1 + 1/M) * mean(n)).
@@ -17,8 +17,9 @@ distribution:  tests/hour = 3600 * slots * B / (T_block * (1 + 1/M) * mean(n)).
   e2e       the same through the C ABI with host buffers: wall-clock kc_batch_step calls (their
             H2D slot tables and work lists, D2H round-off), plus per-test admission (H2D of
             x0 and the tables) and read-back (D2H of the residue), amortised per test
-  roofline  the persistent squaring kernel's algorithmic FP64 FLOPs per launch over its
-            CUDA-event time, against the FP64 FMA peak measured on this GPU by a DFMA kernel
+  roofline  a block's algorithmic FP64 FLOPs (its kernels run concurrently on three streams)
+            over the block's CUDA-event time, against the FP64 FMA peak measured on this GPU
+            by a DFMA kernel
   cpu_baseline  the reference's arithmetic on the host: the CPU oracle's port of the
             reference's `ref` backend (one test per core on all cores) over a bounded sample
 
@@ -181,18 +182,25 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-# squarings of every test per persistent launch (the batch's default, KITE_GB300_STEPS_PER_LAUNCH)
+# parts (streams) of a block's pass launches (the batch's default, KITE_GB300_BATCH_SPLIT)
+PARTS = 3
+# squarings of every test per launch of the persistent kernel, timed beside the block for
+# comparison (the batch's default KITE_GB300_STEPS_PER_LAUNCH)
 STEPS_PER_LAUNCH = 100
-# From one ncu capture of a k_squarings launch (100 squarings of this workload's 256 tests):
+# Per squaring of this workload's 256 tests in the block's form, from one ncu capture of the nine
+# pass launches of one squaring (three parts of three passes; ncu serialises them):
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,sm__sass_thread_inst_executed_op_
-#   {dfma,dadd,dmul}_pred_on.sum,... --clock-control none -k regex:k_squarings -s 12 -c 1
-#   python bench.py --quick --steps 1 --warmup 1 --no-ntt
-# DRAM: 34.99 GB read + 20.57 GB written.  FP64 lane operations executed (DFMA + DADD + DMUL,
-# active lanes): 47.90e9 (33.90e9 + 9.40e9 + 4.60e9).
-K_SQ_DRAM_BYTES = 55.57e9
-K_SQ_FP64_LANE_OPS = 47.90e9
-K_SQ_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_squarings launch, "
-                       "profiles/k_squarings_fermat_batch256.md")
+#   {dfma,dadd,dmul}_pred_on.sum,... --clock-control none -k 'regex:k_rows|k_col_inverse|k_col_forward'
+#   -s 256 -c 9 python bench.py --quick --steps 1 --warmup 1 --no-ntt
+# (the 256 launches skipped are the tests' admission).  A block is B + 1 squaring-sized passes.
+# DRAM: 421.9 MB read + 11.2 MB written (ncu runs the three parts one after another; concurrent,
+# the persistent form of the same passes moved 556 MB per squaring).  FP64 lane operations: 479.0e6
+# per squaring on average, from a 100-squaring capture of the same item functions (the single
+# squaring above, 499.9e6, is a step that also tracks round-off, which one step in four does).
+K_SQ_DRAM_BYTES = 433.1e6
+K_SQ_FP64_LANE_OPS = 479.0e6
+K_SQ_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the nine pass launches of one "
+                       "squaring, times B + 1 (profiles/launches_fermat_batch256.md)")
 
 
 def run_ours(args):
@@ -270,24 +278,27 @@ def run_ours(args):
     e2e_per_test = (t_admit + t_read) / SLOTS + mean_n * ovh * t_block_wall / (SLOTS * BLOCK)
     e2e_value = 3600.0 / e2e_per_test * world
 
-    # ---- roofline (after the timed region, on the same stream): the persistent kernel the
-    #      block runs, and each pass as a kernel of its own for the split of the time
-    msp, flp = C.c_double(), C.c_double()
-    if lib.kc_batch_profile_steps(b.h, STEPS_PER_LAUNCH, C.byref(msp), C.byref(flp)) != 0:
-        raise RuntimeError("kc_batch_profile_steps failed")
+    # ---- roofline (after the timed region): the block's algorithmic FLOPs over its CUDA-event
+    #      time (its kernels overlap on three streams); each pass alone and the persistent kernel,
+    #      on the batch stream, for the split of the time and for comparison
     ms3 = (C.c_double * 3)()
     fl3 = (C.c_double * 3)()
     lib.kc_batch_profile(b.h, 5, ms3, fl3)
+    msp, flp = C.c_double(), C.c_double()
+    if lib.kc_batch_profile_steps(b.h, STEPS_PER_LAUNCH, C.byref(msp), C.byref(flp)) != 0:
+        raise RuntimeError("kc_batch_profile_steps failed")
     peak = lib.kc_fp64_peak(device)
-    sq_name = f"k_squarings (persistent: {STEPS_PER_LAUNCH} squarings of every test per launch)"
-    achieved = flp.value / (msp.value * 1e-3) if msp.value > 0 else 0.0
+    flops_sq = fl3[0] + fl3[1] + fl3[2]          # one squaring of every test
+    flops_block = flops_sq * (BLOCK + 1)          # B squarings and the product
+    achieved = flops_block / t_block
     names = ["k_rows (row FFT + split square), alone", "k_col_inverse (inverse column FFT + round + carry), alone",
              "k_col_forward (carry-in + forward column FFT), alone"]
-    kernels = {sq_name: {"ms_per_launch": msp.value, "gflop_per_launch": flp.value / 1e9,
-                         "tflops": achieved / 1e12}}
-    kernels.update({names[q]: {"ms_per_launch": ms3[q], "gflop_per_launch": fl3[q] / 1e9,
-                               "tflops": fl3[q] / (ms3[q] * 1e-3) / 1e12 if ms3[q] else 0}
-                    for q in range(3)})
+    kernels = {names[q]: {"ms_per_launch": ms3[q], "gflop_per_launch": fl3[q] / 1e9,
+                          "tflops": fl3[q] / (ms3[q] * 1e-3) / 1e12 if ms3[q] else 0}
+               for q in range(3)}
+    kernels[f"k_squarings (persistent form, {STEPS_PER_LAUNCH} squarings of every test per launch)"] = {
+        "ms_per_launch": msp.value, "gflop_per_launch": flp.value / 1e9,
+        "tflops": flp.value / (msp.value * 1e-3) / 1e12 if msp.value else 0}
     b.close()
 
     ntt = ntt_leg(lib, tests, mean_n, device) if args.ntt else None
@@ -347,18 +358,20 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": "tests/hour", "h2d_bytes_per_step": h2d.value,
                     "d2h_bytes_per_step": d2h.value,
                     "admission_s": t_admit, "readback_s": t_read, "block_wall_s": t_block_wall},
-            "gpu_launches": args.steps * (math.ceil(BLOCK / STEPS_PER_LAUNCH) + 3),
+            "gpu_launches": args.steps * (PARTS * 3 * BLOCK + 3),
             "clocks": clk.summary(),
             "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12,
                          "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
-                         "traffic": K_SQ_DRAM_BYTES, "traffic_source": K_SQ_TRAFFIC_SOURCE,
+                         "traffic": K_SQ_DRAM_BYTES * (BLOCK + 1) if K_SQ_DRAM_BYTES else None,
+                         "traffic_source": K_SQ_TRAFFIC_SOURCE,
                          # FP64 instructions actually issued (ncu count) against the probe's
                          # instruction rate (peak / 2: the probe's DFMAs count 2 FLOPs each)
-                         "fp64_issue": {"lane_ops_per_launch": K_SQ_FP64_LANE_OPS,
-                                        "per_second": K_SQ_FP64_LANE_OPS / (msp.value * 1e-3) if msp.value else None,
-                                        "vs_probe_rate": (K_SQ_FP64_LANE_OPS / (msp.value * 1e-3)) / (peak / 2)
-                                        if msp.value and peak else None},
-                         "kernel": sq_name,
+                         "fp64_issue": None if not K_SQ_FP64_LANE_OPS else {
+                             "lane_ops_per_block": K_SQ_FP64_LANE_OPS * (BLOCK + 1),
+                             "per_second": K_SQ_FP64_LANE_OPS * (BLOCK + 1) / t_block,
+                             "vs_probe_rate": K_SQ_FP64_LANE_OPS * (BLOCK + 1) / t_block / (peak / 2) if peak else None},
+                         "kernel": f"one Gerbicz block: the pass kernels of {BLOCK} squarings in {PARTS} parts on "
+                                   f"{PARTS} streams, and the product (one CUDA graph; the unit is the block)",
                          "peak_source": "measured: DFMA dependent-chain kernel on this GPU "
                                         "(MEASURED_PEAKS.json has no FP64 figure)"},
             "kernels": kernels,

@@ -22,15 +22,18 @@ LLR = [
 ]
 
 
-@pytest.mark.parametrize("form", ["auto", "persistent", "per_pass"])
+@pytest.mark.parametrize("form", ["default", "persistent", "two_parts", "one_stream"])
 def test_batch_mixed_fermat_and_llr(lib, monkeypatch, form):
-    """Both forms of a block (the persistent kernel over one queue, and one launch per pass)
-    give the golden verdicts; `auto` lets the batch choose (per pass, for a batch this small)."""
+    """Every form of a block gives the golden verdicts: one launch per pass with the slots in
+    three parts on three streams (the default), in two parts, on one stream, and the persistent
+    kernel over one queue."""
     from ahnum_gb300.kite import Batch, prp
-    if form == "auto":
-        monkeypatch.delenv("KITE_GB300_BATCH_PERSISTENT", raising=False)
-    else:
-        monkeypatch.setenv("KITE_GB300_BATCH_PERSISTENT", "1" if form == "persistent" else "0")
+    monkeypatch.delenv("KITE_GB300_BATCH_PERSISTENT", raising=False)
+    monkeypatch.delenv("KITE_GB300_BATCH_SPLIT", raising=False)
+    if form == "persistent":
+        monkeypatch.setenv("KITE_GB300_BATCH_PERSISTENT", "1")
+    elif form != "default":
+        monkeypatch.setenv("KITE_GB300_BATCH_SPLIT", "2" if form == "two_parts" else "1")
     with Batch(gerbicz_block=200, gerbicz_blocks=20) as b:
         slots = {}
         for k, n, res in FERMAT:
