@@ -105,8 +105,12 @@ int kc_square_noalloc(kc_engine *e, const double *x, double *y);
 /* ---- batched engine ------------------------------------------------------------------------
  * Many independent tests advanced together on one GPU.  The reference's form of concurrent
  * tests is one context per test on CPU threads (`kite throughput`, tools/kite.c:65-105); a batch
- * replaces those contexts: each test is a slot with its own modulus and FFT length, and every
- * kernel launch covers all slots.  Fermat slots run the Gerbicz-checked driver of
+ * replaces those contexts: each test is a slot with its own modulus and FFT length.  A Gerbicz
+ * block of every slot's squarings is one CUDA graph: the slots in three parts of about equal
+ * work, each part's pass launches on its own stream (KITE_GB300_BATCH_SPLIT=P for P parts), or
+ * with KITE_GB300_BATCH_PERSISTENT=1 a persistent kernel over one queue of every slot's work
+ * whose waits between CTAs are bounded (a wait that runs out fails the step with
+ * -cudaErrorLaunchTimeout).  Fermat slots run the Gerbicz-checked driver of
  * src/prp.c:407-567 (block B, check every M blocks, rollback, longer FFT on round-off above
  * 0.40, doubled tail); LLR slots run the doubling V <- V^2 - 2 of src/llr.c:395-406 after the
  * Lucas ladder.  Results are bit-identical to a test run alone. */

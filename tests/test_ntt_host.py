@@ -89,3 +89,19 @@ def test_words_to_limbs_reduces_any_representative(lib):
         back = (C.c_uint64 * nl)()
         assert lib.kn_words_to_limbs(k, n, words, back) == 0
         assert int.from_bytes(C.string_at(back, 8 * nl), "little") == mont * k % N
+
+
+def test_split_members_balances_work_and_keeps_everyone():
+    """NTT groups squared together are dealt members of about equal work (largest first, each
+    to the lightest group); every member lands in exactly one group."""
+    from ahnum_gb300.ntt_group import split_members
+    sizes = [700000, 650000, 300000, 310000, 500000, 480000, 420000]
+    parts = split_members(list(enumerate(sizes)), 2, size=lambda m: m[1])
+    assert len(parts) == 2
+    got = sorted(i for p in parts for i, _ in p)
+    assert got == list(range(len(sizes)))
+    loads = [sum(v for _, v in p) for p in parts]
+    assert abs(loads[0] - loads[1]) <= max(sizes)
+    # more parts than members: one member per part, none empty
+    assert [len(p) for p in split_members([1, 2], 4)] == [1, 1]
+    assert split_members([], 3) == [[]]
