@@ -255,14 +255,6 @@ bool start_fermat(Slot &s, const std::vector<uint64_t> *vx, const std::vector<ui
     return kc_sync(e) == 0;
 }
 
-uint64_t n_mod(uint64_t k, uint64_t n, uint64_t m) {
-    auto mm = [m](uint64_t a, uint64_t c) { return (uint64_t)((unsigned __int128)a * c % m); };
-    uint64_t r = 1 % m, b = 2 % m;
-    for (uint64_t e = n; e; e >>= 1, b = mm(b, b))
-        if (e & 1) r = mm(r, b);
-    return (mm(k % m, r) + m - 1 % m) % m;
-}
-
 // LLR slot: Lucas ladder for V_k(P, -1) on the slot's engine, then V_{2k} = V_k^2 + 2
 // (src/llr.c:150-184, 395-401); the doublings that follow are batched.
 bool start_llr(Slot &s, const std::vector<uint64_t> *vx) {
