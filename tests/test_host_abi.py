@@ -136,3 +136,32 @@ def test_latency_shapes_validated_and_loaded(lib):
                     lib.kc_set_latency_shape(L, 0, 0)
                     lib.kc_set_fft_shape(L, 0)
                     lib.kc_set_fft_time(L, 0.0)
+
+
+def test_length_chooser_respects_the_reference_model(lib):
+    """Every length the chooser picks is a usable four-step length (a multiple of 64 with no
+    prime factor above 7) and holds the test within the reference's bits-per-word model
+    (src/ctx.c:26-33, 107-141), for a seeded spread of k and n."""
+    import random
+    from ahnum_gb300.tune import safe_bpw, usable_lengths
+    rng = random.Random(11)
+    usable = set(usable_lengths(1024, 4 << 20))
+    for _ in range(200):
+        k = rng.randrange(1, 10000) | 1
+        n = int(10 ** rng.uniform(4.3, 7.3))
+        L = lib.kc_choose_fft_len(k, n)
+        assert L in usable, (k, n, L)
+        assert n / L <= safe_bpw(L, k) + 1e-9, (k, n, L)
+
+
+def test_usable_lengths_are_seven_smooth_multiples_of_64():
+    from ahnum_gb300.tune import usable_lengths
+    got = usable_lengths(16384, 20480)
+    # 2^14, 2^7 3^3 5, 2^9 5 7, 2^11 3^2, 2^7 3 7^2, 2^8 3 5^2, 2^6 3^2 5 7, 2^12 5
+    assert got == [16384, 17280, 17920, 18432, 18816, 19200, 20160, 20480]
+    for L in usable_lengths(1 << 16, 1 << 18):
+        x = L
+        for p in (2, 3, 5, 7):
+            while x % p == 0:
+                x //= p
+        assert x == 1 and L % 64 == 0
