@@ -70,7 +70,10 @@ def poisson_requests(seed: int, rate_per_s: float, duration_s: float, fermat_sha
         if t > duration_s:
             return out
         kind = FERMAT if rng.random() < fermat_share else LLR
-        k = int(rng.integers(k_range[0] // 2, k_range[1] // 2 + 1)) * 2 + 1
+        while True:  # k odd and uniform in k_range: an even upper bound's k_range[1] + 1 is redrawn
+            k = int(rng.integers(k_range[0] // 2, k_range[1] // 2 + 1)) * 2 + 1
+            if k <= k_range[1]:
+                break
         n = int(math.exp(rng.uniform(lo, hi)))
         out.append(Request(len(out), kind, k, n, t))
 

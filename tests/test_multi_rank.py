@@ -47,3 +47,4 @@ def test_two_gloo_ranks_take_the_slowest_time():
 def test_single_process_combine_is_identity():
     import bench
     assert bench.combine_ranks(1.5, 2.5, 256, None) == (1.5, 2.5, 1)
+
