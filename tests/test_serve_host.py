@@ -1,5 +1,7 @@
 """Host side of the served request loop (ahnum_gb300/serve.py): the seeded arrival process and
 the FFT-length step a confirmation run takes; no GPU."""
+
+
 def test_served_arrivals_follow_the_workload():
     """The served workload's Poisson arrivals: k odd in [3, 10^4], n log-uniform in
     [10^5, 4 10^6], 80 % Fermat, arrival times increasing within the window, seeded."""
