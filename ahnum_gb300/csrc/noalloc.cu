@@ -3,8 +3,6 @@
 // Every other entry point of the engine keeps its digit and carry scratch in buffers that
 // kc_engine_new allocated.  Some callers cannot allocate device memory at the time they need a
 // squaring:
-//   * code that runs while a stream is being captured into a CUDA graph, where cudaMalloc
-//     would break the capture;
 //   * plugins loaded into a host whose memory pool owns all of the device memory, so a
 //     cudaMalloc of their own fails or evicts the host's data;
 //   * latency-bound loops, where cudaMalloc/cudaFree synchronise the device and stall the
@@ -37,16 +35,26 @@ constexpr size_t kScratchBytes = kDescBytes + kDigBytes + kSlotBytes;
 // The scratch itself: ~0.65 MB per device, shared by every call.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
+// Writes the call's test descriptor into the head of the scratch.  The descriptor travels as a
+// kernel argument, which the launch copies when it is issued, so nothing of the caller's stack
+// frame is read after the call returns and no host staging buffer is involved.
+__global__ void k_noalloc_desc(TestDesc d, TestDesc *dst) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *dst = d;
+}
+
 namespace {
 
 std::mutex g_addr_mu;
 unsigned char *g_addr[kMaxDevices] = {};
 
 // Device address of the scratch array on `device`, looked up once per device with that device
-// current.  The host-side symbol is only a stand-in: passing it to a kernel would fault.
+// current.  The host-side symbol is only a stand-in: passing it to a kernel would fault.  The
+// cached address belongs to the device's primary context: after a cudaDeviceReset the module
+// is loaded again and this cache is stale, so a process that resets a device must not call
+// kc_square_noalloc on it afterwards.
 unsigned char *scratch_address(int device, int *err) {
     if (device < 0 || device >= kMaxDevices) {
-        *err = -1;
+        *err = KC_NOALLOC_BAD_ARGUMENT;
         return nullptr;
     }
     std::lock_guard<std::mutex> lock(g_addr_mu);
@@ -65,13 +73,13 @@ unsigned char *scratch_address(int device, int *err) {
 }  // namespace
 
 extern "C" int kc_square_noalloc(kc_engine *e, const double *x, double *y) {
-    if (!e || !x || !y) return -1;
+    if (!e || !x || !y) return KC_NOALLOC_BAD_ARGUMENT;
     const LengthPlan &P = *e->plan;
     if (e->lay.L > KC_NOALLOC_MAX_WORDS || (size_t)e->NG * P.R * sizeof(long long) > kSlotBytes)
         return KC_NOALLOC_TOO_LARGE;
     int prev = -1;
     cudaGetDevice(&prev);
-    if (prev != e->device && cudaSetDevice(e->device) != cudaSuccess) return -1;
+    if (prev != e->device && cudaSetDevice(e->device) != cudaSuccess) return KC_NOALLOC_BAD_ARGUMENT;
     int rc = 0;
     unsigned char *base = scratch_address(e->device, &rc);
     if (base) {
@@ -83,12 +91,16 @@ extern "C" int kc_square_noalloc(kc_engine *e, const double *x, double *y) {
         d.err_every = 1;
         d.x = nullptr;
         d.y = nullptr;
-        // Nothing here needs clearing between calls: the column inverse kernel writes every
-        // digit and every carry slot before the column forward kernel reads them.
+        // Nothing here needs clearing between calls: the descriptor is rewritten by every call,
+        // and the column inverse kernel writes every digit and every carry slot before the
+        // column forward kernel reads them.
         cudaError_t c = cudaSuccess;
         if (x != y)
             c = cudaMemcpyAsync(y, x, (size_t)e->lay.L * sizeof(double), cudaMemcpyDeviceToDevice, e->stream);
-        if (c == cudaSuccess) c = cudaMemcpyAsync(base, &d, sizeof d, cudaMemcpyHostToDevice, e->stream);
+        if (c == cudaSuccess) {
+            k_noalloc_desc<<<1, 32, 0, e->stream>>>(d, reinterpret_cast<TestDesc *>(base));
+            c = cudaGetLastError();
+        }
         if (c == cudaSuccess) {
             LaunchSet s = e->ls;
             s.tests = reinterpret_cast<const TestDesc *>(base);

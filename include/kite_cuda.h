@@ -87,19 +87,25 @@ int kc_engine_wait_selftest(kc_engine *e, uint64_t wait_cycles);
  * No counterpart in the reference (its backends run on the host and never allocate device
  * memory).  y = x^2 mod N (x == y allowed) on engine e, like kc_square(e, y, 1) after copying x
  * to y, but calling no cudaMalloc, cudaFree or other allocating routine.  It is for callers that
- * cannot allocate when they need the product: code running during a CUDA stream capture, a
- * plugin whose host owns the device memory through its own pool, or a latency-bound loop that
- * cannot afford the device synchronisation of an allocation.  Its scratch is one static device
- * array of about 0.65 MB that every GPU loading this library reserves until the process exits.
+ * cannot allocate when they need the product: a plugin whose host owns the device memory
+ * through its own pool (a cudaMalloc of its own would fail or evict the host's data), or a
+ * latency-bound loop that cannot afford the device synchronisation an allocation brings.  Its
+ * scratch is one static device array of about 0.65 MB that every GPU loading this library
+ * reserves until the process exits.
  *   - lengths above KC_NOALLOC_MAX_WORDS words are refused with KC_NOALLOC_TOO_LARGE;
  *   - the first call on a device looks up the array's device address (cudaGetSymbolAddress)
- *     with that device current: make that first call before any stream capture begins;
- *   - all calls share the array, so calls that overlap on the GPU (different streams, engines
- *     or threads) race and corrupt each other's result: serialise them;
+ *     with that device current and keeps it for the life of the process; after a
+ *     cudaDeviceReset of that device the kept address is stale, so do not call it there again;
+ *   - all calls share the array, which keeps the last call's contents; calls that overlap on
+ *     the GPU (different streams, engines or threads) race and corrupt each other's result:
+ *     serialise them;
  *   - round-off is tracked on every call into the engine's kc_maxerr.
- * Returns 0, KC_NOALLOC_TOO_LARGE, or a negative CUDA error (also recorded on e). */
+ * Returns 0, KC_NOALLOC_TOO_LARGE, KC_NOALLOC_BAD_ARGUMENT (a null argument, or a device this
+ * library cannot address), or a negated CUDA error code (also recorded on e).  The two named
+ * codes lie below -10000, outside the range of negated CUDA errors. */
 #define KC_NOALLOC_MAX_WORDS 65536
-#define KC_NOALLOC_TOO_LARGE (-2)
+#define KC_NOALLOC_TOO_LARGE (-10001)
+#define KC_NOALLOC_BAD_ARGUMENT (-10002)
 int kc_square_noalloc(kc_engine *e, const double *x, double *y);
 
 /* ---- batched engine ------------------------------------------------------------------------

@@ -13,7 +13,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "_build", "libkite_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libkiteref.so")
 REF_CLI = os.path.join(HERE, "_ref", "kite")
-REFERENCE_SRC = "/root/reference"
+# The reference checkout, for building its portable backends (`make ref`): taken from the
+# environment, as the checkout exists only where the fixtures are made, never on a GPU host.
+REFERENCE_SRC = os.environ.get("KITE_REFERENCE_SRC", "")
 
 u64p = C.POINTER(C.c_uint64)
 dp = C.POINTER(C.c_double)
@@ -24,11 +26,12 @@ _lib = None
 
 
 def build(ref: bool | None = None) -> None:
-    """make the oracle; also the reference backends when the reference sources exist."""
+    """make the oracle; also the reference backends when $KITE_REFERENCE_SRC names a checkout."""
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+    have_src = bool(REFERENCE_SRC) and os.path.isdir(os.path.join(REFERENCE_SRC, "src"))
     if ref is None:
-        ref = os.path.isdir(os.path.join(REFERENCE_SRC, "src"))
-    if ref:
+        ref = have_src
+    if ref and have_src:
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REFERENCE_SRC}"], check=True)
 
 
@@ -142,6 +145,9 @@ class OracleCtx:
 
     def maxerr(self) -> float:
         return self.lib.ko_maxerr(self.h)
+
+    def reset_maxerr(self):
+        self.lib.ko_reset_maxerr(self.h)
 
     def layout(self):
         L = self.L

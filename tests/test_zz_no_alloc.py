@@ -1,8 +1,8 @@
 """kc_square_noalloc: the squaring for callers that cannot allocate device memory when they
-need it (during a stream capture, inside a host that owns the device memory through its own
-pool, or in a loop that cannot take an allocation's synchronisation).  Its scratch lives in a
-static device array, so these checks compare it, call after call, with the ordinary
-kc_square, which uses the scratch its engine allocated; the results must be bit-identical.
+need it (a plugin inside a host that owns the device memory through its own pool, or a loop
+that cannot take an allocation's synchronisation).  Its scratch lives in a static device array,
+so these checks compare it, call after call, with the ordinary kc_square, which uses the
+scratch its engine allocated; the results must be bit-identical.
 
 This file is collected last: it runs after every other test, and it also passes alone in a
 fresh process."""
@@ -12,6 +12,10 @@ import random
 import pytest
 
 pytestmark = pytest.mark.gpu
+
+# include/kite_cuda.h: below -10000, apart from negated CUDA error codes
+KC_NOALLOC_TOO_LARGE = -10001
+KC_NOALLOC_BAD_ARGUMENT = -10002
 
 
 def _engine(lib, k, n, L):
@@ -67,7 +71,8 @@ def test_noalloc_refuses_lengths_above_its_maximum(lib):
     e = _engine(lib, 3, 2000000, 131072)
     try:
         x = lib.kc_num_alloc(e)
-        assert lib.kc_square_noalloc(e, x, x) == -2  # KC_NOALLOC_TOO_LARGE
+        assert lib.kc_square_noalloc(e, x, x) == KC_NOALLOC_TOO_LARGE
+        assert lib.kc_square_noalloc(e, None, x) == KC_NOALLOC_BAD_ARGUMENT
         assert lib.kc_error(e) == 0
         lib.kc_num_free(e, x)
     finally:
