@@ -99,6 +99,29 @@ class NttGroup:
         self.close()
 
 
+def residue_nm1(y: int, N: int, base: int) -> int:
+    """base^(N+1) mod N -> base^(N-1) mod N, also when base and N share a factor (the
+    reference's kite_residue_nm1, src/prp.c:63-144): N = Q*M with Q made of the primes of base;
+    the result is 0 mod Q and y / base^2 mod M, joined by the CRT."""
+    q, b, m = 1, base, N
+    p = 2
+    while b > 1:
+        if b % p == 0:
+            while b % p == 0:
+                b //= p
+            while m % p == 0:
+                if q > 1 << 40:
+                    raise ValueError("the base-prime part of N does not fit a word")
+                q *= p
+                m //= p
+        p += 1
+    if q == 1:
+        return y * pow(base * base, -1, N) % N
+    t = y % m * pow(base * base, -1, m) % m
+    u = -t * pow(m, -1, q) % q
+    return t + m * u
+
+
 class NttFermatBatch:
     """Fermat base-a PRP tests of many N = k*2^n-1 on the integer-NTT engine, in lockstep Gerbicz
     blocks: every block squares all tests' x B times (`streams` groups of about equal work, one
@@ -182,9 +205,9 @@ class NttFermatBatch:
         if a != b:
             raise RuntimeError("tail mismatch")
         N = st["N"]
-        r = a * pow(self.base * self.base, -1, N) % N  # base^(N+1) -> base^(N-1)
+        r = residue_nm1(a, N, self.base)
         st["res64"] = r & (2**64 - 1)
-        st["is_prp"] = r == 1
+        st["is_prp"] = a == self.base * self.base
         st["done"] = st["n"]
 
     def run(self, max_blocks: int | None = None):

@@ -56,6 +56,20 @@ def load_gb300_tuning(lib) -> None:
                     lib.kc_set_latency_shape(int(parts[0]), int(parts[2]), int(parts[4]))
 
 
+def unload_gb300_tuning(lib) -> None:
+    """Returns every length of the shipped files to the built-in shapes (engines made afterwards
+    use them; plans already built keep theirs)."""
+    for path, reset in ((THROUGHPUT_FILE, lambda L: lib.kc_set_fft_shape(L, 0)),
+                        (LATENCY_FILE, lambda L: lib.kc_set_latency_shape(L, 0, 0))):
+        if not os.path.exists(path):
+            continue
+        with open(path) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) in (4, 5) and not line.startswith("#"):
+                    reset(int(parts[0]))
+
+
 def usable_lengths(lo: int, hi: int):
     out = []
     for L in range((lo + 63) // 64 * 64, hi + 1, 64):

@@ -268,6 +268,16 @@ def run_ours(args):
     d2h = C.c_uint64()
     lib.kc_batch_last_transfer(b.h, C.byref(h2d), C.byref(d2h))
 
+    # largest round-off of every slot over its blocks so far (warm-up and timed), against the
+    # drivers' 0.40 limit; a slot above it would have been restarted at a longer FFT
+    roundoff = {"max": 0.0, "limit": 0.40, "retries": 0, "gerbicz_errors": 0,
+                "over": f"{args.warmup + args.steps} blocks of every test (warm-up and timed)"}
+    for s in slots:
+        st, r = b.result(s)
+        roundoff["max"] = max(roundoff["max"], r.maxerr)
+        roundoff["retries"] += r.roundoff_retries
+        roundoff["gerbicz_errors"] += r.gerbicz_errors
+
     # ---- read-back of every residue (D2H + exact host conversion), timed for e2e
     t0 = time.perf_counter()
     for (k, n), s in zip(tests, slots):
@@ -308,6 +318,7 @@ def run_ours(args):
             print(json.dumps({"metric": "fermat_tests_per_hour", "value": value, "unit": "tests/hour",
                               "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                               "ms_per_step": t_block * 1e3, "quick": True, "kernels": kernels,
+                              "roundoff": roundoff,
                               "ntt_engine": ntt}), flush=True)
         if dist:
             dist.destroy_process_group()
@@ -358,6 +369,7 @@ def run_ours(args):
             "e2e": {"value": e2e_value, "unit": "tests/hour", "h2d_bytes_per_step": h2d.value,
                     "d2h_bytes_per_step": d2h.value,
                     "admission_s": t_admit, "readback_s": t_read, "block_wall_s": t_block_wall},
+            "roundoff": roundoff,
             "gpu_launches": args.steps * (PARTS * 3 * BLOCK + 3),
             "clocks": clk.summary(),
             "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12,

@@ -105,3 +105,29 @@ def test_split_members_balances_work_and_keeps_everyone():
     # more parts than members: one member per part, none empty
     assert [len(p) for p in split_members([1, 2], 4)] == [1, 1]
     assert split_members([], 3) == [[]]
+
+
+def test_residue_nm1_matches_oracle_with_shared_factors(oracle_mod):
+    """base^(N+1) -> base^(N-1) in the NTT batch's Python finish, against the oracle's restatement
+    of the reference's kite_residue_nm1, including N divisible by primes of the base"""
+    import ctypes as C
+    import random
+    from ahnum_gb300.ntt_group import residue_nm1
+    lib = oracle_mod.load()
+    rng = random.Random(5)
+    shared = 0
+    for _ in range(150):
+        k = rng.randrange(1, 3000) | 1
+        n = rng.randrange(60, 400)
+        N = k * (1 << n) - 1
+        for base in (3, 5, 6, 15):
+            y = rng.randrange(N)
+            nl = (n + 127) // 64
+            arr = (C.c_uint64 * nl)(*[(y >> (64 * i)) & (2**64 - 1) for i in range(nl)])
+            Narr = (C.c_uint64 * nl)(*[(N >> (64 * i)) & (2**64 - 1) for i in range(nl)])
+            rc = lib.ko_residue_nm1(arr, Narr, nl, base)
+            want = sum(int(arr[i]) << (64 * i) for i in range(nl))
+            assert rc == 0
+            assert residue_nm1(y, N, base) == want, (k, n, base)
+            shared += N % 3 == 0 or N % 5 == 0
+    assert shared > 0
