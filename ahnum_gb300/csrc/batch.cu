@@ -60,8 +60,8 @@ struct Slot {
 };
 
 size_t slot_bytes(uint32_t L, uint32_t R, uint32_t NG) {
-    // six numbers, digit scratch, tables (bits, w, osc, idig), carry slots
-    return (size_t)L * (6 * 8 + 8 + 1 + 3 * 8) + (size_t)NG * R * 8 + 4096;
+    // six numbers, two digit vectors, tables (bits, w, osc, idig), carry slots
+    return (size_t)L * (6 * 8 + 2 * 8 + 1 + 3 * 8) + (size_t)NG * R * 8 + 4096;
 }
 
 }  // namespace
@@ -87,6 +87,8 @@ struct kc_batch {
                                  // [2 ..] parts 1 .. of a split block
     unsigned long long *h_err = nullptr;  // pinned, one per slot
     int cap_err = 0;
+    int *d_eq = nullptr, *h_eq = nullptr;  // zero-test verdicts of the slots compared this block
+    int cap_eq = 0;
     cudaGraphExec_t graph = nullptr;
     size_t graph_row_smem = 0, graph_col_smem = 0;
     uint32_t graph_B = 0;
@@ -312,11 +314,30 @@ bool start_llr(Slot &s, const std::vector<uint64_t> *vx) {
     return kc_sync(e) == 0;
 }
 
-bool numbers_equal(Slot &s, const double *a, const double *c) {
+// The verdict of a comparison queued on the device this block (1 equal, 0 different); 2 (the
+// device carry did not settle) falls back to canonical limbs on the host.
+bool numbers_equal(Slot &s, const double *a, const double *c, int verdict) {
+    if (verdict == 0 || verdict == 1) return verdict == 1;
     const size_t nl = s.e->lay.nlimbs;
     std::vector<uint64_t> la(nl), lc(nl);
     if (kc_get_limbs(s.e, a, la.data()) || kc_get_limbs(s.e, c, lc.data())) return false;
     return la == lc;
+}
+
+// the pair a slot compares after this block's products: d with x0 * t^(2^B) in its check, x
+// with t after the doubled tail
+bool compared_pair(Slot &s, const double *&a, const double *&c) {
+    if (s.phase == Phase::Check) {
+        a = s.t;
+        c = s.d;
+        return true;
+    }
+    if (s.phase == Phase::TailT) {
+        a = s.x;
+        c = s.t;
+        return true;
+    }
+    return false;
 }
 
 void finish_fermat(Slot &s) {
@@ -580,6 +601,8 @@ void kc_batch_free(kc_batch *b) {
         if (b->pstream[p]) cudaStreamSynchronize(b->pstream[p]);
     for (auto &l : b->lists) free_lists(l);
     if (b->h_err) cudaFreeHost(b->h_err);
+    cudaFree(b->d_eq);
+    if (b->h_eq) cudaFreeHost(b->h_eq);
     if (b->h_flow) cudaFreeHost(b->h_flow);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
@@ -725,6 +748,26 @@ int kc_batch_step(kc_batch *b, uint32_t blocks, double *gpu_ms) {
             launch_col_forward(ms, nullptr, true, 0);
             bok(b, cudaGetLastError());
         }
+        // ---- comparisons on the device: the check's d == x0 * t^(2^B) and the tail's x == t,
+        //      one verdict word per slot read back with the round-off
+        if ((int)b->slots.size() > b->cap_eq) {
+            cudaFree(b->d_eq);
+            if (b->h_eq) cudaFreeHost(b->h_eq);
+            b->d_eq = b->h_eq = nullptr;
+            b->cap_eq = (int)b->slots.size() * 2 + 16;
+            if (!bok(b, cudaMalloc((void **)&b->d_eq, b->cap_eq * sizeof(int))) ||
+                !bok(b, cudaMallocHost((void **)&b->h_eq, b->cap_eq * sizeof(int))))
+                return b->err;
+        }
+        for (size_t i = 0; i < b->slots.size(); i++) {
+            Slot &s = b->slots[i];
+            const double *a, *c;
+            if (!active(s) || !compared_pair(s, a, c)) continue;
+            kc_queue_equal(s.e, b->stream, a, c, b->d_eq + i);
+            bok(b, cudaGetLastError());
+            bok(b, cudaMemcpyAsync(&b->h_eq[i], b->d_eq + i, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+            b->d2h += sizeof(int);
+        }
         bok(b, cudaEventRecord(b->ev1, b->stream));
         // ---- round-off of every slot of this block
         if ((int)b->slots.size() > b->cap_err) {
@@ -773,7 +816,7 @@ int kc_batch_step(kc_batch *b, uint32_t blocks, double *gpu_ms) {
                 if (s.round_blocks >= b->M || s.i >= s.full) s.phase = Phase::Check;
                 break;
             case Phase::Check:
-                if (numbers_equal(s, s.t, s.d)) {
+                if (numbers_equal(s, s.t, s.d, b->h_eq[i])) {
                     s.consecutive_fail = 0;
                     s.vi = s.i;
                     kc_copy(s.e, s.vx, s.x);
@@ -806,7 +849,7 @@ int kc_batch_step(kc_batch *b, uint32_t blocks, double *gpu_ms) {
                 s.phase = Phase::TailT;
                 break;
             case Phase::TailT:
-                if (numbers_equal(s, s.x, s.t)) {
+                if (numbers_equal(s, s.x, s.t, b->h_eq[i])) {
                     finish_fermat(s);
                 } else if (++s.tail_attempts > 5) {
                     s.res.rc = -3;
@@ -877,6 +920,19 @@ int kc_batch_checkpoint(kc_batch *b, int slot, const char *path) {
     h.fft_len = s.res.fft_len;
     h.run = 0;
     return llr_checkpoint_write(path, h, vx) ? 0 : -1;
+}
+
+int kc_batch_debug_corrupt(kc_batch *b, int slot) {
+    if (slot < 0 || slot >= (int)b->slots.size() || !active(b->slots[slot])) return -1;
+    cudaSetDevice(b->device);
+    if (!bok(b, cudaStreamSynchronize(b->stream))) return b->err;
+    Slot &s = b->slots[slot];
+    const uint32_t L = s.e->lay.L;
+    std::vector<int64_t> d(L);
+    if (kc_to_digits(s.e, s.x, d.data())) return -1;
+    d[L / 3] += 1;
+    if (kc_from_digits(s.e, s.x, d.data())) return -1;
+    return kc_sync(s.e) ? -1 : 0;
 }
 
 void kc_batch_last_transfer(const kc_batch *b, uint64_t *h2d, uint64_t *d2h) {

@@ -38,6 +38,14 @@ int kc_set_limbs(kc_engine *e, double *x, const uint64_t *limbs) {
     return kc_from_digits(e, x, d.data());
 }
 
+void kc_queue_equal(kc_engine *e, cudaStream_t stream, const double *a, const double *b, int *flag) {
+    LaunchSet s = e->ls;
+    s.stream = stream;
+    launch_col_digits(s, (const double2 *)a, e->d_dig);
+    launch_col_digits(s, (const double2 *)b, e->d_dig2);
+    launch_equal(stream, e->d_desc, 0, e->d_dig, e->d_dig2, flag);
+}
+
 int kc_mul_small_host(kc_engine *e, double *x, int64_t m) {
     std::vector<int64_t> d(e->lay.L);
     if (kc_to_digits(e, x, d.data())) return e->err ? e->err : -1;
@@ -83,6 +91,9 @@ void release(kc_engine *e) {
     cudaFree(e->d_osc);
     cudaFree(e->d_idig);
     cudaFree(e->d_dig);
+    cudaFree(e->d_dig2);
+    cudaFree(e->d_eq);
+    if (e->h_eq) cudaFreeHost(e->h_eq);
     cudaFree(e->d_slot);
     cudaFree(e->d_maxerr);
     cudaFree(e->d_status);
@@ -234,7 +245,9 @@ kc_engine *kc_engine_create(uint64_t k, uint64_t n, uint32_t L, const uint8_t *b
     bool good = ok(e, cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking)) &&
                 dalloc(e, &e->d_desc, 1) && dalloc(e, &e->d_work, P.pairs.size() + e->NG) &&
                 dalloc(e, &e->d_bits, L) && dalloc(e, &e->d_w, L) && dalloc(e, &e->d_osc, L) &&
-                dalloc(e, &e->d_idig, L) && dalloc(e, &e->d_dig, L) && dalloc(e, &e->d_slot, (size_t)e->NG * P.R) &&
+                dalloc(e, &e->d_idig, L) && dalloc(e, &e->d_dig, L) && dalloc(e, &e->d_dig2, L) &&
+                dalloc(e, &e->d_eq, 1) && ok(e, cudaMallocHost((void **)&e->h_eq, sizeof(int))) &&
+                dalloc(e, &e->d_slot, (size_t)e->NG * P.R) &&
                 dalloc(e, &e->d_maxerr, 1) && dalloc(e, &e->d_status, 1) &&
                 ok(e, cudaMallocHost((void **)&e->h_dig, (size_t)L * sizeof(long long))) &&
                 ok(e, cudaMallocHost((void **)&e->h_err, sizeof(unsigned long long)));
@@ -366,6 +379,21 @@ int kc_to_digits(kc_engine *e, const double *x, int64_t *digits) {
         return e->err;
     std::memcpy(digits, e->h_dig, L * sizeof(long long));
     return 0;
+}
+
+int kc_equal(kc_engine *e, const double *a, const double *b) {
+    DeviceGuard dg(e->device);
+    if (a == b) return 1;
+    kc_queue_equal(e, e->stream, a, b, e->d_eq);
+    if (!check_launch(e) ||
+        !ok(e, cudaMemcpyAsync(e->h_eq, e->d_eq, sizeof(int), cudaMemcpyDeviceToHost, e->stream)) ||
+        !ok(e, cudaStreamSynchronize(e->stream)))
+        return e->err;
+    if (*e->h_eq != 2) return *e->h_eq;
+    // the device carry did not settle within its bounds: compare canonical limbs on the host
+    std::vector<uint64_t> la(e->lay.nlimbs), lb(e->lay.nlimbs);
+    if (kc_get_limbs(e, a, la.data()) || kc_get_limbs(e, b, lb.data())) return e->err ? e->err : -1;
+    return la == lb ? 1 : 0;
 }
 
 int kc_square(kc_engine *e, double *x, uint64_t count) {

@@ -23,6 +23,8 @@ struct kc_engine {
     uint8_t *d_bits = nullptr;
     double *d_w = nullptr, *d_osc = nullptr, *d_idig = nullptr;
     long long *d_dig = nullptr, *d_slot = nullptr;
+    long long *d_dig2 = nullptr;     // second digit vector of the zero test (kc_equal)
+    int *d_eq = nullptr, *h_eq = nullptr;  // its verdict, on the device and pinned
     unsigned long long *d_maxerr = nullptr;
     int *d_status = nullptr;
     long long *h_dig = nullptr;      // pinned staging for digit transfers
@@ -58,3 +60,6 @@ bool kc_ok(kc_engine *e, cudaError_t rc);
 int kc_get_limbs(kc_engine *e, const double *x, uint64_t *limbs);   // canonical, waits
 int kc_set_limbs(kc_engine *e, double *x, const uint64_t *limbs);
 int kc_mul_small_host(kc_engine *e, double *x, int64_t m);
+// Queues the zero test of a - b (mod N) on `stream`: the digits of a into e->d_dig, of b into
+// e->d_dig2, the verdict (1 equal, 0 different, 2 undetermined) into *flag.
+void kc_queue_equal(kc_engine *e, cudaStream_t stream, const double *a, const double *b, int *flag);

@@ -497,7 +497,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_squarings(const TestDe
 template <int G>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_digits(const TestDesc *__restrict__ tests,
                                                          const WorkItem *__restrict__ work,
-                                                         int nwork, const double2 *xo) {
+                                                         int nwork, const double2 *xo, long long *digo) {
     extern __shared__ double2 sm[];
     __shared__ TestDesc s_desc;
     pdl_enter();
@@ -505,6 +505,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_digits(const TestD
         const WorkItem it = work[wi];
         const TestDesc &T = stage_desc(tests, it.test, &s_desc);
         const double2 *x = xo ? xo : T.x;
+        long long *dig = digo ? digo : T.dig;
         const int R = T.R, C = T.C, g = it.unit;
         load_columns_conj<G>(T, x, g, sm);
         __syncthreads();
@@ -512,12 +513,120 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_col_digits(const TestD
         for (int i = threadIdx.x; i < R * G; i += blockDim.x) {
             const int r = i / G, l = i % G;
             const int j = 2 * (r * C + g * G + l);
-            T.dig[j] = llrint(sm[i].x * T.idig[j]);
-            T.dig[j + 1] = llrint(sm[i].y * T.idig[j + 1]);
+            dig[j] = llrint(sm[i].x * T.idig[j]);
+            dig[j + 1] = llrint(sm[i].y * T.idig[j + 1]);
         }
         __syncthreads();
     }
     pdl_leave();
+}
+
+// Zero test of a - b modulo N for two digit vectors of one test (the digits of two numbers, as
+// k_col_digits leaves them): the Gerbicz check's comparison d == x0 * t^(2^B) and the tail's
+// x == t, done where the numbers live.  The reference compares canonical limbs on the host
+// (src/prp.c:291-296 and :470-474, via kite_get_limbs).
+//
+// The difference e = a - b is carried exactly as a whole number: the low digits (below top_t)
+// are balanced in kEqualThreads chunks, each chunk's carry-out moving to the next chunk round
+// by round until none is left; the top region (digits top_t..L-1 with the carry out of the low
+// digits) is folded by k*2^n == 1 and re-centred (fold_top), and the fold's amount for digit 0
+// rippled in the same way.  Afterwards every low digit is balanced and the top region lies in
+// [-k 2^m/2, k 2^m/2), so |e| < N and e == 0 (mod N) exactly when every digit is zero.
+// *flag = 1 (equal), 0 (not equal), or 2 when the carry did not settle within its bounds (the
+// caller then compares on the host).  a is overwritten; one CTA per test.
+constexpr int kEqualThreads = 512;
+
+__device__ __forceinline__ long long ripple(long long *e, const uint8_t *bits, int j0, int j1, long long c) {
+    for (int j = j0; j < j1 && c; j++) {
+        const int b = bits[j];
+        const long long v = e[j] + c;
+        c = (v + (1ll << (b - 1))) >> b;
+        e[j] = v - (c << b);
+    }
+    return c;
+}
+
+__global__ void __launch_bounds__(kEqualThreads) k_equal_mod_n(const TestDesc *__restrict__ tests, int test,
+                                                               long long *__restrict__ a,
+                                                               const long long *__restrict__ b, int *flag) {
+    __shared__ long long s_out[kEqualThreads];  // carry out of chunk i, not yet moved on
+    __shared__ long long s_in0;                  // carry into chunk 0 (from the fold)
+    __shared__ long long s_top;                  // carry out of the low digits into the top region
+    __shared__ int s_more;
+    const TestDesc &T = tests[test];
+    const int L = T.L, t = T.top_t, tid = threadIdx.x, nt = blockDim.x;
+    for (int j = tid; j < L; j += nt) a[j] -= b[j];
+    // chunks of the low digits [0, t): nch chunks of cs digits (the last one may be shorter)
+    const int cs = (t + nt - 1) / nt, nch = (t + cs - 1) / cs;
+    const int j0 = min(t, tid * cs), j1 = min(t, j0 + cs);
+    if (tid == 0) {
+        s_in0 = 0;
+        s_top = 0;
+    }
+    __syncthreads();
+    // every chunk balanced on its own, from no carry
+    long long c = 0;
+    if (tid < nch) {
+        for (int j = j0; j < j1; j++) {
+            const int bw = T.bits[j];
+            const long long v = a[j] + c;
+            c = (v + (1ll << (bw - 1))) >> bw;
+            a[j] = v - (c << bw);
+        }
+        s_out[tid] = c;
+    }
+    int settled = 0;
+    for (int pass = 0; pass < 64; pass++) {
+        // move the carries on until every chunk has absorbed its carry-in; a carry advances at
+        // least one chunk per round, so nch + 1 rounds always suffice
+        int quiet = 0;
+        for (int round = 0; round <= nch + 1; round++) {
+            __syncthreads();
+            const long long cin = tid == 0 ? s_in0 : (tid < nch ? s_out[tid - 1] : 0);
+            const long long to_top = s_out[nch - 1];
+            __syncthreads();
+            if (tid == 0) {
+                s_in0 = 0;
+                s_top += to_top;
+            }
+            long long r = 0;
+            if (tid < nch) {
+                r = ripple(a, T.bits, j0, j1, cin);
+                s_out[tid] = r;
+            }
+            if (!__syncthreads_or(r != 0)) {
+                quiet = 1;
+                break;
+            }
+        }
+        if (!quiet) break;  // not settled within the bound: undetermined
+        // fold the top region (always once, again whenever a carry reached it)
+        if (tid == 0) {
+            const long long add = s_top;
+            s_top = 0;
+            s_more = 0;
+            if (pass == 0 || add) {
+                long long q;
+                if (t < L) {
+                    a[t] += add;
+                    q = fold_top(T, a, 0);
+                } else {
+                    q = fold_top(T, a, add);
+                }
+                s_in0 = q;
+                s_more = q != 0;
+            }
+        }
+        __syncthreads();
+        if (!s_more) {
+            settled = 1;
+            break;
+        }
+    }
+    int nonzero = 0;
+    for (int j = tid; j < L; j += nt) nonzero |= a[j] != 0;
+    nonzero = __syncthreads_or(nonzero);
+    if (tid == 0) *flag = settled ? (nonzero ? 0 : 1) : 2;
 }
 
 // x op= y element-wise over n complex values: 0 copy, 1 add, 2 sub
@@ -679,12 +788,16 @@ int launch_squarings(const LaunchSet &s, unsigned *flow, int step0, int nsteps, 
     return 0;
 }
 
-void launch_col_digits(const LaunchSet &s, const double2 *x) {
+void launch_col_digits(const LaunchSet &s, const double2 *x, long long *dig) {
     switch (s.G) {
-    case 2: launch_pass(k_col_digits<2>, s.grid_cols, s.threads, s.col_smem, s.stream, s.tests, s.cols, s.ncols, x); break;
-    case 4: launch_pass(k_col_digits<4>, s.grid_cols, s.threads, s.col_smem, s.stream, s.tests, s.cols, s.ncols, x); break;
-    default: launch_pass(k_col_digits<8>, s.grid_cols, s.threads, s.col_smem, s.stream, s.tests, s.cols, s.ncols, x); break;
+    case 2: launch_pass(k_col_digits<2>, s.grid_cols, s.threads, s.col_smem, s.stream, s.tests, s.cols, s.ncols, x, dig); break;
+    case 4: launch_pass(k_col_digits<4>, s.grid_cols, s.threads, s.col_smem, s.stream, s.tests, s.cols, s.ncols, x, dig); break;
+    default: launch_pass(k_col_digits<8>, s.grid_cols, s.threads, s.col_smem, s.stream, s.tests, s.cols, s.ncols, x, dig); break;
     }
+}
+
+void launch_equal(cudaStream_t st, const TestDesc *tests, int test, long long *a, const long long *b, int *flag) {
+    k_equal_mod_n<<<1, kEqualThreads, 0, st>>>(tests, test, a, b, flag);
 }
 
 void launch_elementwise(cudaStream_t st, double2 *x, const double2 *y, size_t n, int op) {

@@ -53,7 +53,12 @@ void launch_fp64_probe(cudaStream_t st, int grid, int block, int iters, double *
 // The probe with `chains` chains per thread (4, 8 or 16 for DFMA; 8 for DMUL and DADD) of
 // opcode op (0 DFMA, 1 DMUL, 2 DADD); -1 for a combination it does not have.
 int launch_fp64_probe_var(cudaStream_t st, int grid, int block, int iters, int chains, int op, double *out);
-void launch_col_digits(const LaunchSet &s, const double2 *x);
+// The digits of x (every test of the set's column list) into each test's dig scratch, or into
+// `dig` when it is given (a single-test set).
+void launch_col_digits(const LaunchSet &s, const double2 *x, long long *dig = nullptr);
+// Zero test of a - b (mod N) for digit vectors of test `test` of the table (k_equal_mod_n, one
+// CTA): *flag = 1 equal, 0 different, 2 undetermined (compare on the host).  a is overwritten.
+void launch_equal(cudaStream_t st, const TestDesc *tests, int test, long long *a, const long long *b, int *flag);
 // Squarings step0 .. step0+nsteps-1 of every test of the lists in one persistent launch
 // (k_squarings) of `grid` CTAs.  `flow` holds kFlowDone + (tests) words, zeroed before the
 // launch.  A CTA that waits longer than wait_limit SM cycles for another's item raises

@@ -136,6 +136,7 @@ PROTOTYPES = {
     "kc_copy": (C.c_int, [vp, vp, vp]),
     "kc_add": (C.c_int, [vp, vp, vp]),
     "kc_sub": (C.c_int, [vp, vp, vp]),
+    "kc_equal": (C.c_int, [vp, vp, vp]),
     "kc_maxerr": (C.c_double, [vp]),
     "kc_reset_maxerr": (None, [vp]),
     "kc_set_roundoff_check": (None, [vp, C.c_uint32]),
@@ -165,6 +166,7 @@ PROTOTYPES = {
     "kc_batch_read": (C.c_int, [vp, C.c_int, u64p]),
     "kc_batch_checkpoint": (C.c_int, [vp, C.c_int, C.c_char_p]),
     "kc_batch_last_transfer": (None, [vp, u64p, u64p]),
+    "kc_batch_debug_corrupt": (C.c_int, [vp, C.c_int]),
     "kc_set_fft_shape": (C.c_int, [C.c_uint32, C.c_uint32]),
     "kc_set_fft_time": (None, [C.c_uint32, C.c_double]),
     "kc_fft_shape_candidates": (C.c_int, [C.c_uint32, u32p, u32p, C.c_int]),

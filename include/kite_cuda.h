@@ -53,6 +53,13 @@ int kc_mul(kc_engine *e, double *x, const double *y);
  * V <- V^2 - 2, src/llr.c:395-406), the constant folded into the carry: no extra pass. */
 int kc_square_add(kc_engine *e, double *x, uint64_t count, int64_t c);
 
+/* a == b (mod N)?  Replaces the canonical comparison of the reference's drivers (nums_equal,
+ * src/prp.c:291-296, used by the Gerbicz check at src/prp.c:470-474 and the tail at :538),
+ * which converts both numbers to limbs on the host.  Here the digits of a and b are formed on
+ * the device, their difference is carried exactly with the top fold, and only the verdict (4
+ * bytes) comes back.  Waits for the queue.  1 equal, 0 different, or a negative CUDA error. */
+int kc_equal(kc_engine *e, const double *a, const double *b);
+
 /* Replace the host loops of kite_copy / kite_add / kite_sub (src/ctx.c:323-343). */
 int kc_copy(kc_engine *e, double *dst, const double *src);
 int kc_add(kc_engine *e, double *x, const double *y);
@@ -160,6 +167,10 @@ int kc_batch_read(kc_batch *b, int slot, uint64_t *limbs);
  * KITECKP1 (x and d limbs, src/prp.c:158-192) for Fermat slots, KITELLR1 (V limbs, run 0,
  * src/llr.c:106-121) for LLR slots.  0, or -1 on failure. */
 int kc_batch_checkpoint(kc_batch *b, int slot, const char *path);
+/* Testing hook, the batch's form of kite_debug_corrupt (src/prp.c:28-34): adds 1 to digit L/3
+ * of the slot's current x, a valid encoding of a wrong value that only the Gerbicz check (or the
+ * tail's comparison) catches.  0, or -1 when the slot is not running. */
+int kc_batch_debug_corrupt(kc_batch *b, int slot);
 /* Host<->device bytes moved by the last kc_batch_step (slot tables, work lists, round-off). */
 void kc_batch_last_transfer(const kc_batch *b, uint64_t *h2d, uint64_t *d2h);
 /* Free a slot's device memory (its number becomes reusable by later admissions). */
