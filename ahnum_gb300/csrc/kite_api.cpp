@@ -40,6 +40,16 @@ int kite_square_add_internal(kite_ctx *ctx, kite_num *x, uint64_t count, int64_t
     return ctx->ntt ? kn_square_add(ctx->ntt, wd(x), count, c) : kc_square_add(ctx->eng, fp(x), count, c);
 }
 
+int kite_equal_internal(kite_ctx *ctx, const kite_num *a, const kite_num *b) {
+    if (!ctx->ntt) return kc_equal(ctx->eng, fp(a), fp(b));
+    std::vector<uint64_t> la(ctx->lay.nlimbs), lb(ctx->lay.nlimbs);
+    const int rc = kn_get_limbs(ctx->ntt, wd(a), la.data());
+    if (rc) return rc;
+    const int rc2 = kn_get_limbs(ctx->ntt, wd(b), lb.data());
+    if (rc2) return rc2;
+    return la == lb ? 1 : 0;
+}
+
 extern "C" {
 
 kite_ctx *kite_ctx_new(uint64_t k, uint64_t n, int32_t c, const kite_opts *o) {

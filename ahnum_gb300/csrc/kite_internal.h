@@ -22,3 +22,6 @@ struct kite_num {
 
 // x <- x^2 + c, count times, on the context's engine (the LLR doubling with c = -2)
 int kite_square_add_internal(kite_ctx *ctx, kite_num *x, uint64_t count, int64_t c);
+// a == b (mod N): decided on the device by the FP64 engine (kc_equal: 4 bytes read back), by
+// canonical limbs for the integer-NTT engine.  1 equal, 0 different, negative on a CUDA error.
+int kite_equal_internal(kite_ctx *ctx, const kite_num *a, const kite_num *b);

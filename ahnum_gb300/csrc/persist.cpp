@@ -114,4 +114,12 @@ bool llr_checkpoint_read(const char *path, size_t nlimbs, LlrCheckpointHeader &h
     return true;
 }
 
+bool llr_checkpoint_header(const char *path, LlrCheckpointHeader &h) {
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return false;
+    const bool ok = std::fread(&h, sizeof h, 1, f) == 1 && !std::memcmp(h.magic, kLlrMagic, 8);
+    std::fclose(f);
+    return ok;
+}
+
 }  // namespace kg

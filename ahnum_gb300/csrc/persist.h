@@ -30,5 +30,8 @@ bool prp_checkpoint_header(const char *path, PrpCheckpointHeader &h);
 
 bool llr_checkpoint_write(const char *path, const LlrCheckpointHeader &h, const std::vector<uint64_t> &x);
 bool llr_checkpoint_read(const char *path, size_t nlimbs, LlrCheckpointHeader &h, std::vector<uint64_t> &x);
+// The header alone (magic checked, checksum not), as the reference's kite_llr_checkpoint_iter
+// reads it (src/llr.c:135-146).
+bool llr_checkpoint_header(const char *path, LlrCheckpointHeader &h);
 
 }  // namespace kg

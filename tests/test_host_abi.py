@@ -165,3 +165,23 @@ def test_usable_lengths_are_seven_smooth_multiples_of_64():
             while x % p == 0:
                 x //= p
         assert x == 1 and L % 64 == 0
+
+
+def test_llr_choose_P_matches_oracle(lib, oracle_mod):
+    """P = the smallest P >= 1 with Jacobi(P^2+4 | N) != 1, and the factor of 4P(P^2+4) and N,
+    from the library's word-size symbol (N mod 4a) against the oracle's restatement of the
+    reference (src/llr.c:33-93), over seeded k, n including small and huge n"""
+    import ctypes as C
+    import random
+    rng = random.Random(77)
+    lo = oracle_mod.load()
+    factors = 0
+    for _ in range(400):
+        k = rng.randrange(1, 1 << 20) | 1
+        n = rng.choice([rng.randrange(3, 200), rng.randrange(200, 10**6), rng.randrange(10**6, 10**8)])
+        P1, f1 = C.c_uint32(), C.c_uint64()
+        P2, f2 = C.c_uint32(), C.c_uint64()
+        assert lib.kite_llr_choose_P(k, n, C.byref(P1), C.byref(f1)) == lo.ko_llr_choose_P(k, n, C.byref(P2), C.byref(f2))
+        assert (P1.value, f1.value) == (P2.value, f2.value), (k, n)
+        factors += f1.value != 0
+    assert factors > 0

@@ -115,3 +115,34 @@ def test_read_rejects_bad_files(lib, tmp_path):
     os.remove(tmp_path / "f.md5")
     assert lib.pp_read(str(p).encode(), native.PP_TYPE_VALUE, fpP, C.byref(it), g, 1) != 0
     assert lib.pp_read(str(tmp_path / "missing").encode(), native.PP_TYPE_VALUE, fpP, C.byref(it), g, 1) != 0
+
+
+def _reference_points(iterations, count):
+    """PRST's point positions as the reference's loop computes them (src/prstproof.c:191-207),
+    restated here as the checker of the library's closed form"""
+    pos = [0] * (count + 1)
+    M = 0
+    for i in range(1, count):
+        M = iterations
+        j = count // 2
+        while j > 0 and (i & (j * 2 - 1)) != 0:
+            M //= 2
+            if i & j:
+                pos[i] += M
+            if iterations & (count // j // 2):
+                pos[i] += 1
+            j //= 2
+    pos[count] = iterations
+    return pos, M
+
+
+def test_points_closed_form_matches_the_reference_loop(lib):
+    import random
+    rng = random.Random(3)
+    for _ in range(300):
+        count = 1 << rng.randrange(1, 11)
+        iterations = rng.choice([rng.randrange(count, 5000), rng.randrange(10**5, 2**31 - 1)])
+        pos = (C.c_uint32 * (count + 1))()
+        M = lib.pp_points(iterations, count, pos)
+        want, wM = _reference_points(iterations, count)
+        assert list(pos) == want and M == wM, (iterations, count)
