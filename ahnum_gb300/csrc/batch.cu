@@ -95,6 +95,8 @@ struct kc_batch {
     int grid = 0;
     int threads = 128;  // block size of the pass kernels
     bool persistent = false;      // squaring blocks as the persistent kernel k_squarings
+    bool stagger = false;         // first rounds of 1..M blocks by admission order (kc_batch_stagger_checks)
+    uint64_t admitted = 0;        // Fermat slots admitted so far
     int parts = 3;                // per-pass blocks of 2+ tests in this many parts, one stream each
     int form = -1;                // the form of the captured block graph (BlockForm)
     int graph_parts = 0;          // its number of parts
@@ -653,6 +655,10 @@ static int admit(kc_batch *b, int kind, uint64_t k, uint64_t n, uint32_t base, u
     ok = ok && open_engine(b, s, L);
     if (ok) ok = kind == KC_TEST_FERMAT ? start_fermat(s, nullptr, nullptr) : start_llr(s, nullptr);
     if (ok) s.full = s.n / b->B * b->B;
+    // staggered checks: the first round of the j-th admitted Fermat slot is 1 + (j mod M) blocks,
+    // so the slots' checks spread evenly over the blocks instead of falling on the same one
+    if (ok && kind == KC_TEST_FERMAT && b->stagger) s.round_blocks = b->M - 1 - (uint32_t)(b->admitted % b->M);
+    if (ok && kind == KC_TEST_FERMAT) b->admitted++;
     if (!ok) {
         release_slot(b, s);
         s.used = false;
@@ -668,6 +674,8 @@ int kc_batch_add_fermat(kc_batch *b, uint64_t k, uint64_t n, uint32_t base, uint
 int kc_batch_add_llr(kc_batch *b, uint64_t k, uint64_t n, uint32_t fft_len) {
     return admit(b, KC_TEST_LLR, k, n, 0, fft_len);
 }
+
+void kc_batch_stagger_checks(kc_batch *b, int on) { b->stagger = on != 0; }
 
 int kc_batch_active(const kc_batch *b) {
     int c = 0;
@@ -885,6 +893,7 @@ int kc_batch_result(const kc_batch *b, int slot, kc_test_result *out) {
     if (out) {
         *out = s.res;
         out->iter = s.vi;
+        out->position = s.phase == Phase::Done ? s.n : s.i;
         out->fft_len = s.res.fft_len;
     }
     if (s.phase == Phase::Done) return 1;

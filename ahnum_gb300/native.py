@@ -76,7 +76,7 @@ class KcTestResult(C.Structure):
                 ("maxerr", C.c_double), ("gerbicz_errors", C.c_uint32),
                 ("roundoff_retries", C.c_uint32), ("squarings", C.c_uint64),
                 ("seconds", C.c_double), ("P", C.c_uint32), ("factor", C.c_uint64),
-                ("iter", C.c_uint64)]
+                ("iter", C.c_uint64), ("position", C.c_uint64)]
 
 
 KITE_BACKEND_CUDA = 5
@@ -167,6 +167,7 @@ PROTOTYPES = {
     "kc_batch_checkpoint": (C.c_int, [vp, C.c_int, C.c_char_p]),
     "kc_batch_last_transfer": (None, [vp, u64p, u64p]),
     "kc_batch_debug_corrupt": (C.c_int, [vp, C.c_int]),
+    "kc_batch_stagger_checks": (None, [vp, C.c_int]),
     "kc_set_fft_shape": (C.c_int, [C.c_uint32, C.c_uint32]),
     "kc_set_fft_time": (None, [C.c_uint32, C.c_double]),
     "kc_fft_shape_candidates": (C.c_int, [C.c_uint32, u32p, u32p, C.c_int]),

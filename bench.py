@@ -8,12 +8,14 @@ reference publishes no benchmark suite.
 
 A step is one Gerbicz block of every test: B = 1000 squarings of each test's x (one CUDA graph:
 the tests in three parts of about equal work, each part's 3000 pass launches on its own stream)
-plus the block's product d <- d*x.  The check of every M = 250
-blocks (another B squarings and a product) is charged analytically, as a factor (1 + 1/M).
-Throughput is the steady state of a served batch whose slots are refilled with tests of the same
-distribution:  tests/hour = 3600 * slots * B / (T_block * (1 + 1/M) * mean(n)).
+plus the block's product d <- d*x, and for the tests at the end of a round the check (B
+squarings of t and a product instead of x's, then the comparison on the device).  The first
+round of the j-th test is 1 + (j mod M) blocks (kc_batch_stagger_checks), so the checks fall on
+different blocks as in a batch refilled over time, and every timed block holds the steady
+state's share of them.  Throughput is measured progress: tests/hour = 3600 * (squarings of x
+advanced by all tests) / (T_blocks * mean(n)).
 
-  value     T_block from CUDA events around the work on the batch stream
+  value     T_blocks from CUDA events around the work on the batch stream
   e2e       the same through the C ABI with host buffers: wall-clock kc_batch_step calls (their
             H2D slot tables and work lists, D2H round-off), plus per-test admission (H2D of
             x0 and the tables) and read-back (D2H of the residue), amortised per test
@@ -47,6 +49,15 @@ BLOCK = 1000
 BLOCKS_PER_CHECK = 250
 SEED = 3
 WORKLOAD = "fermat-batch-256: k odd U[3,1e4], n U[300000,700000], base 3, B=1000, M=250"
+
+
+def bench_config(lengths: dict, mean_n: float) -> dict:
+    """The workload as both arms report it (the reference arm computes the same lengths)."""
+    return {"workload": WORKLOAD, "slots": SLOTS, "mean_n": mean_n,
+            "fft_lengths": {str(k): v for k, v in sorted(lengths.items())},
+            "checks": f"Gerbicz check every M={BLOCKS_PER_CHECK} blocks, first rounds staggered by "
+                      "admission order (check work inside the timed blocks)",
+            "l2": "inputs larger than L2 (~256 x 0.3 MB numbers + 0.6 MB tables per test)"}
 
 
 def workload(seed: int = SEED, count: int = SLOTS):
@@ -154,32 +165,49 @@ def run_reference(args):
     rank, world, _ = rank_info()
     if rank != 0:
         return
+    from oracle import oracle
+    oracle.build(ref=False)
     threads = os.cpu_count() or 1
     tests = workload()
+    mean_n = statistics.mean(n for _, n in tests)
+    lengths = {}
+    for k, n in tests:
+        L = oracle.choose_fft_len(k, n)
+        lengths[L] = lengths.get(L, 0) + 1
     sample = tests[:threads]
+    squarings = 64
     # each step: one test per core, a bounded number of squarings each
     for _ in range(args.warmup):
         cpu_sample(sample, threads, 4)
-    vals, secs = [], []
+    vals = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        tph, work, det = cpu_sample(sample, threads, 16)
+        tph, work, det = cpu_sample(sample, threads, squarings)
         vals.append(tph)
-        secs.append(work)
     wall = time.perf_counter() - t0
     value = statistics.median(vals)
+    desc = (f"{len(sample)} of the 256 tests (one per core) x {squarings} squarings per step, "
+            "extrapolated to full tests (n squarings, Gerbicz overhead 1/M + 2/B)")
     line = {
         "impl": "reference", "metric": "fermat_tests_per_hour", "value": value,
         "unit": "tests/hour", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": wall * 1e3 / max(args.steps, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64)",
-        "config": {"workload": WORKLOAD, "sample": f"{len(sample)} tests x 16 squarings per step"},
+        "config": bench_config(lengths, mean_n),
         "cpu_baseline": {"value": value, "unit": "tests/hour", "cores": threads, "kind": "port",
-                         "sample": f"{len(sample)} tests (one per core) x 16 squarings per step, "
-                                   "extrapolated to full tests"},
+                         "sample": desc, "note": PORT_NOTE},
         "e2e": {"value": value, "unit": "tests/hour", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+# The reference's own `ref` backend cannot be built on the GPU host (its sources stay in the build
+# container and binaries built there do not run on the Arm host), so the CPU figure is the
+# oracle's port of it.  Measured single-threaded in the build container (oracle/_ref built from
+# the reference sources): ref 8.15 / 10.2 / 17.3 ms per squaring at L = 28672 / 36864 / 49152,
+# the port 2.03 / 2.31 / 3.01 ms: the port is 4.0-5.8x faster, so this baseline favours the CPU.
+PORT_NOTE = ("the oracle's port of the reference's ref backend; in the build container the port "
+             "was 4.0-5.8x faster per squaring than the reference's own ref build (L 28672-49152)")
 
 
 # parts (streams) of a block's pass launches (the batch's default, KITE_GB300_BATCH_SPLIT)
@@ -228,6 +256,7 @@ def run_ours(args):
 
     # ---- admission (H2D of x0 digits and tables), timed for e2e
     b = Batch(gerbicz_block=BLOCK, gerbicz_blocks=BLOCKS_PER_CHECK, device=device)
+    lib.kc_batch_stagger_checks(b.h, 1)
     t0 = time.perf_counter()
     slots = [b.add_fermat(k, n) for k, n in tests]
     t_admit = time.perf_counter() - t0
@@ -241,7 +270,11 @@ def run_ours(args):
     for _ in range(args.warmup):
         b.step(1)
 
+    def positions():
+        return [b.result(s)[1].position for s in slots]
+
     # ---- timed region: K blocks, events on the batch stream, barrier + max over ranks
+    before = positions()
     if dist:
         dist.barrier()
     gpu_ms = []
@@ -257,11 +290,12 @@ def run_ours(args):
             gpu_ms.append(ms.value)
     if dist:
         dist.barrier()
+    progress = sum(a - p for a, p in zip(positions(), before))  # squarings of x advanced
+    check_blocks = (SLOTS * BLOCK * args.steps - progress) / BLOCK
     t_block, t_block_wall, _ = combine_ranks(statistics.mean(gpu_ms) * 1e-3, statistics.mean(wall),
                                              SLOTS, dist)
 
-    ovh = 1 + 1 / BLOCKS_PER_CHECK
-    per_rank = 3600.0 * SLOTS * BLOCK / (t_block * ovh * mean_n)
+    per_rank = 3600.0 * progress / (t_block * args.steps * mean_n)
     value = per_rank * world
 
     h2d = C.c_uint64()
@@ -285,7 +319,7 @@ def run_ours(args):
         if lib.kc_batch_read(b.h, s, limbs) != 0:
             raise RuntimeError("kc_batch_read failed")
     t_read = time.perf_counter() - t0
-    e2e_per_test = (t_admit + t_read) / SLOTS + mean_n * ovh * t_block_wall / (SLOTS * BLOCK)
+    e2e_per_test = (t_admit + t_read) / SLOTS + mean_n * t_block_wall * args.steps / progress
     e2e_value = 3600.0 / e2e_per_test * world
 
     # ---- roofline (after the timed region): the block's algorithmic FLOPs over its CUDA-event
@@ -355,7 +389,8 @@ def run_ours(args):
         tph, work, det = cpu_sample(tests[:threads], threads, args.cpu_squarings)
         cpu = {"value": tph, "unit": "tests/hour", "cores": threads, "kind": "port",
                "sample": f"{det['tests']} of the 256 tests, one per core, {det['squarings_each']} "
-                         f"squarings each ({work:.1f} s of CPU work), extrapolated to full tests"}
+                         f"squarings each ({work:.1f} s of CPU work), extrapolated to full tests",
+               "note": PORT_NOTE}
 
     if rank == 0:
         line = {
@@ -363,9 +398,9 @@ def run_ours(args):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t_block * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded PCG64)",
-            "config": {"workload": WORKLOAD, "slots": SLOTS, "mean_n": mean_n,
-                       "fft_lengths": {str(k): v for k, v in sorted(lengths.items())},
-                       "l2": "inputs larger than L2 (~256 x 0.3 MB numbers + 0.6 MB tables per test)"},
+            "config": bench_config(lengths, mean_n),
+            "timed_progress": {"squarings_of_x": progress, "check_blocks": check_blocks,
+                               "blocks": args.steps},
             "e2e": {"value": e2e_value, "unit": "tests/hour", "h2d_bytes_per_step": h2d.value,
                     "d2h_bytes_per_step": d2h.value,
                     "admission_s": t_admit, "readback_s": t_read, "block_wall_s": t_block_wall},

@@ -146,6 +146,7 @@ typedef struct {
     uint32_t P;                /* LLR */
     uint64_t factor;           /* LLR: small factor found while choosing P */
     uint64_t iter;             /* last verified iteration */
+    uint64_t position;         /* squarings of x done so far (n once finished) */
 } kc_test_result;
 
 /* gerbicz_block 0: 1000; gerbicz_blocks 0: max(block/4, 8); mem_budget 0: 80% of free memory. */
@@ -155,6 +156,12 @@ void kc_batch_free(kc_batch *b);
  * invalid test, -2 when the memory budget is full. */
 int kc_batch_add_fermat(kc_batch *b, uint64_t k, uint64_t n, uint32_t base, uint32_t fft_len);
 int kc_batch_add_llr(kc_batch *b, uint64_t k, uint64_t n, uint32_t fft_len);
+/* Spread the Gerbicz checks of the Fermat slots admitted from now on: the first round of the
+ * j-th admitted slot is 1 + (j mod M) blocks instead of M, so in a batch admitted at once the
+ * slots' checks fall on different blocks, as they do in a batch refilled over time.  Every round
+ * still ends in the reference's check (src/prp.c:407-517); a shorter first round only adds one.
+ * Verdicts do not change.  Off by default. */
+void kc_batch_stagger_checks(kc_batch *b, int on);
 /* Advance every active slot by `blocks` Gerbicz blocks (B squarings each, plus the block's
  * product or check).  *gpu_ms receives the CUDA-event time of the work.  Returns the number of
  * slots still active, or a negative CUDA error. */

@@ -2,9 +2,9 @@
 
 bench.py times the batched engine with the shipped GB300 four-step shapes
 (ahnum_gb300/tuning_gb300.txt), Gerbicz blocks of B = 1000 squarings with a check every M = 250
-blocks, and the default block form (the slots in three parts, each part's pass launches on its
-own stream, one CUDA graph per block).  These tests build the batch exactly that way and run
-full Fermat tests to their RES64:
+blocks (first rounds staggered by admission order), and the default block form (the slots in
+three parts, each part's pass launches on its own stream, one CUDA graph per block).  These
+tests build the batch exactly that way and run full Fermat tests to their RES64:
 
   * the reference's golden residues at the batched sizes: the 14 primecrunch rows at
     n = 369502..369717 (reference tests/known_residues.csv:14-27) and the known primes
@@ -52,8 +52,11 @@ def bench_shapes(lib):
 
 
 def _bench_batch():
+    from ahnum_gb300 import native
     from ahnum_gb300.kite import Batch
-    return Batch(gerbicz_block=bench.BLOCK, gerbicz_blocks=bench.BLOCKS_PER_CHECK)
+    b = Batch(gerbicz_block=bench.BLOCK, gerbicz_blocks=bench.BLOCKS_PER_CHECK)
+    native.load().kc_batch_stagger_checks(b.h, 1)  # as bench.py: first rounds of 1..M blocks
+    return b
 
 
 def _run_to_verdicts(b, tests):
