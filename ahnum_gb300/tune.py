@@ -223,6 +223,37 @@ def roundoff_report(lengths, k: int = 9999, squarings: int = 500, seed: int = 1)
     return rows
 
 
+def bpw_limit(lib, L: int, k: int, threshold: float, squarings: int, seed: int = 1, step: float = 0.05) -> float:
+    """The largest bits per word (to `step`) at which the round-off of `squarings` squarings of a
+    seeded residue at length L stays at or below `threshold`: the reference's fitting method
+    (tools/fit_bpw.py, bisection from its model's guess), run on these kernels."""
+    guess = (53 - 6 - 0.5 * math.log2(L) - math.log2(k)) / 2
+    lo, hi = guess - 3, guess + 4
+    while hi - lo > step:
+        mid = (lo + hi) / 2
+        e = lib.kc_roundoff_probe(k, int(mid * L), L, squarings, seed)
+        if 0 <= e <= threshold:
+            lo = mid
+        else:
+            hi = mid
+    return lo
+
+
+def fit_bpw(lengths, ks, threshold: float = 0.25, squarings: int = 300):
+    """bpw_limit over a grid of lengths and multipliers, and the least-squares fit of the
+    reference's model form bpw = a - b (log2 L - 12) - c log2 k.  Returns (rows, (a, b, c))."""
+    import numpy as np
+    lib = native.load()
+    rows = []
+    for L in lengths:
+        for k in ks:
+            rows.append((L, k, bpw_limit(lib, L, k, threshold, squarings)))
+    A = np.array([[1.0, -(math.log2(L) - 12), -math.log2(k)] for L, k, _ in rows])
+    y = np.array([b for _, _, b in rows])
+    coef = np.linalg.lstsq(A, y, rcond=None)[0]
+    return rows, tuple(float(v) for v in coef)
+
+
 def main():
     ap = argparse.ArgumentParser()
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -239,6 +270,12 @@ def main():
     c.add_argument("--out")
     f = sub.add_parser("fp64", help="the FP64 probe in several shapes and opcodes (lane ops per second)")
     f.add_argument("--device", type=int, default=0)
+    g = sub.add_parser("fitbpw", help="fit the safe bits-per-word model to these kernels")
+    g.add_argument("--lengths", type=int, nargs="+",
+                   default=[4096, 16384, 20480, 24576, 28672, 32768, 36864, 40960, 49152, 65536, 262144, 1048576])
+    g.add_argument("--ks", type=int, nargs="+", default=[1, 3, 31, 255, 2047, 9999])
+    g.add_argument("--threshold", type=float, default=0.25)
+    g.add_argument("--squarings", type=int, default=300)
     b = sub.add_parser("roundoff")
     b.add_argument("lengths", type=int, nargs="+")
     b.add_argument("--k", type=int, default=9999)
@@ -255,6 +292,17 @@ def main():
             name = ("DFMA", "DMUL", "DADD")[op]
             tf = f"{2 * r / 1e12:.4f}" if op == 0 else "-"
             print(f"| {name} | {chains} | {bps} x {thr} | {r / 1e9:.1f} | {tf} |", flush=True)
+        return
+    if args.cmd == "fitbpw":
+        rows, (a, b_, c) = fit_bpw(args.lengths, args.ks, args.threshold, args.squarings)
+        print(f"| L | k | largest bpw with maxerr <= {args.threshold} over {args.squarings} squarings | "
+              "reference model without its 0.2 margin |")
+        print("|---|---|---|---|")
+        for L, k, bpw in rows:
+            ref = safe_bpw(L, k) + 0.2
+            print(f"| {L} | {k} | {bpw:.2f} | {ref:.2f} |", flush=True)
+        print(f"\nfit: bpw = {a:.3f} - {b_:.4f} (log2 L - 12) - {c:.4f} log2 k   "
+              f"(reference: 21.44 - 0.305 (log2 L - 12) - 0.5 log2 k, then 0.2 below)")
         return
     if args.cmd == "shapes":
         out = open(args.out, "w") if args.out else None
