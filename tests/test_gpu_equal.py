@@ -20,7 +20,7 @@ def _engine(lib, k, n, L=0):
 
 def _from_int(lib, e, k, n, L, v):
     nl = (n + 127) // 64
-    limbs = (C.c_uint64 * nl)(*[(v >> (64 * i)) & (2**64 - 1) for i in range(nl)])
+    limbs = (C.c_uint64 * nl).from_buffer_copy(v.to_bytes(8 * nl, "little"))
     d = (C.c_int64 * L)()
     assert lib.kc_limbs_to_digits(k, n, L, limbs, d) == 0
     x = lib.kc_num_alloc(e)
@@ -73,15 +73,23 @@ def test_equal_against_integers(lib, k, n, L):
         assert lib.kc_equal(e, x, z) == 0
         assert lib.kc_equal(e, z, x) == 0
         assert lib.kc_equal(e, x, w) == 0
-        # products that agree as residues: (v^2)^2 from two squarings vs v^4 set from limbs
+        # products that agree as residues: (v^2)^2 from two squarings, against v^4 set from
+        # limbs (Python integers, up to a million bits) and against two multiplications (the
+        # product kernels, which leave other digit vectors)
         sq = lib.kc_num_alloc(e)
         nums.append(sq)
         assert lib.kc_copy(e, sq, x) == 0
         assert lib.kc_square(e, sq, 2) == 0
-        p4, _ = _from_int(lib, e, k, n, L, pow(v, 4, N))
-        nums.append(p4)
-        assert lib.kc_equal(e, sq, p4) == 1
-        assert lib.kc_equal(e, p4, sq) == 1
+        if n <= 1_000_000:
+            p4, _ = _from_int(lib, e, k, n, L, pow(v, 4, N))
+            nums.append(p4)
+            assert lib.kc_equal(e, sq, p4) == 1
+            assert lib.kc_equal(e, p4, sq) == 1
+        m4, y = lib.kc_num_alloc(e), lib.kc_num_alloc(e)
+        nums += [m4, y]
+        assert lib.kc_copy(e, m4, x) == 0 and lib.kc_copy(e, y, x) == 0
+        assert lib.kc_mul(e, m4, y) == 0 and lib.kc_copy(e, y, m4) == 0 and lib.kc_mul(e, m4, y) == 0
+        assert lib.kc_equal(e, sq, m4) == 1
         # digits hold the stored value x/k: the digit vector of -1 is x = -k (mod N)
         mk, _ = _from_int(lib, e, k, n, L, N - k)
         neg = _from_digits(lib, e, [-1] + [0] * (L - 1))
