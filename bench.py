@@ -405,7 +405,9 @@ def run_ours(args):
                     "d2h_bytes_per_step": d2h.value,
                     "admission_s": t_admit, "readback_s": t_read, "block_wall_s": t_block_wall},
             "roundoff": roundoff,
-            "gpu_launches": args.steps * (PARTS * 3 * BLOCK + 3),
+            # per block: the three passes of each part, the block's product (three passes), and
+            # per check block two digit passes and the comparison kernel
+            "gpu_launches": int(args.steps * (PARTS * 3 * BLOCK + 3) + 3 * check_blocks),
             "clocks": clk.summary(),
             "roofline": {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12,
                          "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
